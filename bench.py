@@ -1,0 +1,332 @@
+"""Benchmark of the GB300 hot path: fused Lax-Wendroff step + track deposition.
+
+Workload (default): the 5 um full-electrode chamber -- 56.2 MeV/u protons,
+300 V over 0.2 cm, 540 us pulses at 50 Hz, 8.91 Gy/s, sampled radius 0.265 cm,
+seed 1: a 1068 x 1068 x 406 grid (463 M voxels, 7.4 GB of float32 fields
+double-buffered), 25 057 919 tracks per pulse over 2 948 pulse steps. A timed
+step is one time step inside the first pulse: the step's ~8 500 tracks
+deposited and the whole grid swept.
+
+Metric: interior voxel-steps per second (interior = (no_xy-2)^2 (nzb-2), the
+reference's unit, profiling/bench_gh200.py:191). The fields (7.4 GB) are far
+larger than the 129 MB L2, so every step streams from HBM; no L2 flush is
+needed between steps.
+
+Lines printed (rank 0, one JSON object each):
+  --impl gb300 (default): value (device-resident inputs), e2e through
+    run_simulation_b200 (host sampling, H2D of tracks, D2H of tallies), the
+    step kernel's roofline against the measured HBM copy bandwidth, the FP64
+    CPU oracle timed on a bounded sample as cpu_baseline, SM clocks sampled
+    during the timed region.
+  --impl reference: the FP64 CPU oracle (the reference's algorithm restated
+    in C with OpenMP) on the same workload, on all host cores.
+
+Multi-GPU (torchrun, one rank per GPU): independent replicas of the workload,
+no collective on the data path; value = all ranks' voxel-steps / max time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+PACKAGE = "iontracks-pulsedproton-python_gb300"
+BYTES_PER_VOXEL_STEP = 16  # float32: read n+ and n-, write both next fields
+
+BEAM = dict(E_MeV_u=56.2, voltage_V=300.0, electrode_gap_cm=0.2, pulse_duration_s=540e-6,
+            repetition_rate_hz=50.0, dose_rate_Gy_s=8.91)
+WORKLOADS = {
+    # name: (description, SimulationConfig kwargs)
+    "full_electrode_5um": ("5 um full electrode, r=0.265 cm, 1068x1068x406, 10 pulses, seed 1",
+                           dict(BEAM, grid_size_um=5.0, sampled_radius_cm=0.265, n_pulses=10, seed=1,
+                                max_voxels=2e9)),
+    "column_5um_r05": ("5 um column, r=0.05 cm, 208x208x406, 8.91 Gy/s, seed 1",
+                       dict(BEAM, grid_size_um=5.0, sampled_radius_cm=0.05, seed=1, max_voxels=2e9)),
+    "column_10um_r008": ("10 um column, r=0.008 cm, 24x24x206, seed 1",
+                         dict(BEAM, grid_size_um=10.0, sampled_radius_cm=0.008, seed=1)),
+}
+
+
+def _pkg():
+    return importlib.import_module(PACKAGE)
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return world, rank
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _traffic_bytes(workload):
+    """dram bytes per step-kernel launch from the committed ncu summary."""
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    return d.get(workload, {}).get("dram_bytes_per_launch")
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.proc = None
+        self.gpu = gpu_index
+        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _config(workload):
+    desc, kw = WORKLOADS[workload]
+    return desc, _pkg().SimulationConfig(**kw)
+
+
+def _interior(cfg):
+    return (cfg.no_xy - 2) ** 2 * (cfg.no_z_with_buffer - 2)
+
+
+def cpu_sample(cfg, steps=2, threads=None):
+    """FP64 oracle (the reference algorithm in C/OpenMP) on the first
+    ``steps`` pulse steps of the workload; returns (voxel-steps/s, cores)."""
+    from oracle import oracle
+
+    cores = threads or oracle.cores_used()
+    oracle.set_threads(cores)
+    t0 = time.perf_counter()
+    res = oracle.run(cfg, mode="batched", max_steps=steps, keep_fields=False)
+    _ = time.perf_counter() - t0
+    return _interior(cfg) * res["steps"] / res["wall_s"], cores, res["wall_s"]
+
+
+def run_reference(args):
+    world, rank = _dist()
+    if rank != 0:
+        return 0
+    desc, cfg = _config(args.workload)
+    steps = max(1, args.ref_steps)
+    vals = []
+    cores = None
+    for _ in range(args.warmup if args.warmup < 1 else 0):
+        pass
+    v, cores, wall = cpu_sample(cfg, steps=steps)
+    vals.append(v)
+    line = {
+        "impl": "reference", "metric": "interior voxel-steps/s", "value": v, "unit": "voxel-steps/s",
+        "n_gpus": world, "steps": steps, "warmup": 0, "ms_per_step": wall / steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": desc},
+        "cpu_baseline": {"value": v, "unit": "voxel-steps/s", "cores": cores, "kind": "port",
+                         "sample": f"first {steps} pulse steps of the workload (deposition + sweep), FP64 oracle"},
+        "e2e": {"value": v, "unit": "voxel-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args):
+    import torch
+    import torch.distributed as dist
+
+    world, rank = _dist()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    pkg = _pkg()
+    eng_mod = importlib.import_module(PACKAGE + ".engine")
+    native = importlib.import_module(PACKAGE + "._native")
+    desc, cfg = _config(args.workload)
+    rng = np.random.default_rng(cfg.seed + rank)
+    sched = pkg.build_track_schedule(cfg, rng)
+    n_steps = args.warmup + args.steps
+    if n_steps > cfg.pulse_time_steps:
+        raise SystemExit("warmup + steps must fit in the first pulse")
+    counts = sched[:n_steps]
+    xs, ys = pkg.TrackSampler(rng, cfg.mid_xy, cfg.sampling_radius, cfg.no_xy).sample(int(counts.sum()))
+    eng = eng_mod.ChamberEngine(cfg, dtype=args.dtype, max_tracks=len(xs), tally_steps=n_steps)
+    eng.upload_tracks(xs, ys, non_blocking=False)
+    off = np.zeros(n_steps + 1, dtype=np.int64)
+    np.cumsum(counts, out=off[1:])
+    stream = torch.cuda.current_stream()
+
+    # warm-up steps, then K timed steps
+    eng.run_segment(off[: args.warmup + 1])
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        t_start.record(stream)
+        eng.run_segment(off[args.warmup:] - off[args.warmup], track_base=int(off[args.warmup]))
+        t_end.record(stream)
+        torch.cuda.synchronize()
+    ms = t_start.elapsed_time(t_end)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    vox = _interior(cfg)
+    value = vox * args.steps * world / (ms / 1e3)
+    launches = 2 * int((counts[args.warmup:] > 0).sum()) + int((counts[args.warmup:] == 0).sum())
+
+    # dominant kernel: the fused step, one launch per step, event-timed on
+    # its own stream, with this step's deposition density applied
+    import ctypes
+
+    g = eng.grid
+    lib = native.load()
+    reps = max(5, min(50, args.steps))
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    cur = eng.parity
+    for r in range(reps):
+        evs[r][0].record(stream)
+        rc = lib.pic_step(ctypes.byref(g), eng.pos[cur].data_ptr(), eng.neg[cur].data_ptr(),
+                          eng.pos[cur ^ 1].data_ptr(), eng.neg[cur ^ 1].data_ptr(), eng.dens[0].data_ptr(), None,
+                          eng.tally[0].data_ptr(), eng.workspace.data_ptr(), eng.workspace.numel(),
+                          stream.cuda_stream)
+        native.check(rc, "pic_step")
+        evs[r][1].record(stream)
+        cur ^= 1
+    torch.cuda.synchronize()
+    step_ms = statistics.median(a.elapsed_time(b) for a, b in evs)
+    peak, peak_kind = _peaks()
+    achieved = BYTES_PER_VOXEL_STEP * vox / (step_ms / 1e3) / 1e9
+    traffic = _traffic_bytes(args.workload)
+    eng.close()
+    del eng
+    torch.cuda.empty_cache()
+
+    # end to end through the public solver call (host sampling, H2D tracks,
+    # D2H tallies), the same steps as the device-resident timing
+    e2e = None
+    if rank == 0 or world > 1:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = pkg.run_simulation_b200(cfg, rng=np.random.default_rng(cfg.seed + rank), progress=False,
+                                      max_steps=args.e2e_steps, return_fields=False)
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+        tracks = float(sched[: args.e2e_steps].sum())
+        e2e = {"value": vox * res.steps_completed * world / e2e_s, "unit": "voxel-steps/s",
+               "h2d_bytes_per_step": 16.0 * tracks / args.e2e_steps, "d2h_bytes_per_step": 32,
+               "steps": int(res.steps_completed), "wall_s": e2e_s,
+               "includes": "schedule + track sampling on the host, H2D of tracks, all steps, D2H of tallies"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        v, cores, wall = cpu_sample(cfg, steps=args.ref_steps)
+        cpu = {"value": v, "unit": "voxel-steps/s", "cores": cores, "kind": "port",
+               "sample": f"first {args.ref_steps} pulse steps of the same workload, FP64 oracle, {wall:.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": "interior voxel-steps/s", "value": value, "unit": "voxel-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.dtype == "float32" else "f64",
+            "data": "synthetic",
+            "config": {"workload": desc, "grid": [cfg.no_xy, cfg.no_xy, cfg.no_z_with_buffer],
+                       "interior_voxels": vox, "tracks_in_timed_steps": int(counts[args.warmup:].sum()),
+                       "l2": "fields 7.4 GB >> 129 MB L2: every step streams from HBM, no flush needed"
+                       if args.workload == "full_electrode_5um" else "inputs smaller than L2",
+                       "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                         "kernel": "step_kernel", "kernel_ms": step_ms,
+                         "algorithmic_bytes_per_launch": BYTES_PER_VOXEL_STEP * vox},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="full_electrode_5um")
+    ap.add_argument("--dtype", choices=["float32", "float64"], default="float32")
+    ap.add_argument("--e2e-steps", type=int, default=600)
+    ap.add_argument("--ref-steps", type=int, default=2)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        raise SystemExit("--warmup must be >= 3")
+    return run_reference(args) if args.impl == "reference" else run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

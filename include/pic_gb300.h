@@ -1,0 +1,159 @@
+/*
+ * pic_gb300.h -- C ABI of the GB300 (sm_103a) hot path of the pulsed-proton
+ * ion-chamber recombination solver.
+ *
+ * Plain pointers and sizes only. Every device pointer is a CUDA device
+ * address owned by the caller (the Python host allocates with PyTorch and
+ * passes Tensor.data_ptr()); streams are cudaStream_t passed as uintptr_t
+ * (0 = legacy default stream). Every entry point returns PIC_OK (0) or a
+ * negative PIC_E_* code; pic_last_error() then describes the failure (the
+ * message is per host thread). No C++ exception crosses this boundary.
+ *
+ * Field layout in HBM: one array per species and buffer,
+ *     field[i][j][k],  0 <= i, j < no_xy,  0 <= k < kpitch,
+ * k fastest, kpitch = pic_kpitch(nzb) >= nzb (rows start 32-byte aligned).
+ * Elements k >= nzb - 1 and k == 0 are the z end planes plus padding and are
+ * kept at zero. Fields are float32 (PIC_F32) or float64 (PIC_F64, the
+ * validation build); the 2D density follows the field type. Per-step tallies
+ * are always float64: tally[s] = {injected, recombined, sum n+, sum n-} over
+ * the scored voxels.
+ */
+#ifndef PIC_GB300_H
+#define PIC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PIC_OK 0
+#define PIC_E_INVALID (-1)  /* bad argument: size, alignment, null pointer */
+#define PIC_E_CUDA (-2)     /* a CUDA runtime call failed */
+#define PIC_E_DEVICE (-3)   /* no usable sm_103 device */
+#define PIC_E_CAPACITY (-4) /* a size beyond what the entry point supports */
+
+#define PIC_F32 0
+#define PIC_F64 1
+
+#define PIC_WALL_ABSORBING 0
+#define PIC_WALL_REFLECTING 1
+
+/* One grid and the scalars its kernels need. Mirrors the attributes of the
+ * reference's SimulationConfig that its kernels take as arguments
+ * (pulsed_ion_chamber/solver_numba.py:54-68, :130-151). */
+typedef struct pic_grid {
+    int64_t no_xy;          /* lateral size (both axes)                      */
+    int64_t nzb;            /* no_z_with_buffer: k extent incl. electrodes   */
+    int64_t kpitch;         /* allocated k extent, pic_kpitch(nzb)           */
+    int64_t no_z;           /* gap layers                                    */
+    int64_t nze;            /* no_z_electrode: first gap layer               */
+    double mid_xy;          /* grid centre (float; odd no_xy gives .5)       */
+    double scoring_radius_sq;
+    double p_lat, p_zm, p_zp, p_cen; /* positive-species LW weights          */
+    double n_lat, n_zm, n_zp, n_cen; /* negative species, applied z-swapped  */
+    double alpha_dt;        /* recombination alpha * dt                      */
+    double gaussian_factor; /* N0 / (pi b^2), track peak density             */
+    double h2_over_b2;      /* voxel area / track radius^2                   */
+    double cutoff_voxels;   /* deposition half-width                         */
+    int32_t wall;           /* PIC_WALL_*                                    */
+    int32_t dtype;          /* PIC_F32 or PIC_F64                            */
+} pic_grid;
+
+/* Description of the last failure on this host thread ("" if none). */
+const char *pic_last_error(void);
+
+/* ABI version (bumped on any signature change). */
+int pic_abi_version(void);
+
+/* k pitch for a given no_z_with_buffer: nzb rounded up to 8 elements. */
+int64_t pic_kpitch(int64_t nzb);
+
+/* Checks that a CUDA device of compute capability 10.3 is current; fills the
+ * SM count and the device's total memory. */
+int pic_device_info(int32_t *sm_count, int64_t *total_bytes, int32_t *cc_major, int32_t *cc_minor);
+
+/* Bytes of device scratch the fused step needs for this grid (per-block
+ * tally partials and a completion counter). The caller allocates it once,
+ * zero-filled, and passes it to pic_step / pic_run_segment. */
+int pic_step_workspace_bytes(const pic_grid *g, int64_t *bytes);
+
+/*
+ * pic_deposit -- sum one step's track Gaussians into the 2D density.
+ *
+ * dens[i][j] += sum_t exp(-(i-x_t)^2 h2/b2) exp(-(j-y_t)^2 h2/b2) over each
+ * track's truncated stencil box [ceil(x-cut), floor(x+cut)] clipped to the
+ * grid (dimensionless; the gaussian factor is applied by pic_step), and
+ * counts[int(x)][int(y)] += 1 per track. dens must be zero on entry for a
+ * fresh step (pic_step zeroes the next step's buffer).
+ *
+ * Replaces: _insert_track_numba's per-track stencil (solver_numba.py:84-98),
+ * _precompute_track_gaussians + _build_row_index +
+ * _accumulate_track_density_numba_parallel (solver_numba_parallel.py:421-457,
+ * :140-180, :183-219), _accumulate_kernel (solver_cuda.py:291-323) and
+ * Diagnostics.count_tracks (state.py:71-84).
+ */
+int pic_deposit(const pic_grid *g, const double *xs, const double *ys, int64_t n_tracks, void *dens,
+                uint32_t *counts, uintptr_t stream);
+
+/*
+ * pic_step -- one fused time step: deposition broadcast, Lax-Wendroff sweep,
+ * recombination sink, lateral wall and the step's tallies.
+ *
+ * Reads pos_in/neg_in (+ gaussian_factor * dens in every gap layer when dens
+ * is non-null), writes every column of pos_out/neg_out: the interior by the
+ * 7-point Lax-Wendroff stencil minus alpha*dt*n+*n-, the outer ring carried
+ * with the step's deposition (absorbing) or mirrored from the new interior
+ * (reflecting). Writes tally[0..3] = {injected, recombined, sum n+, sum n-}
+ * over the scored voxels. If dens_zero is non-null it is zero-filled (the
+ * buffer the next step's pic_deposit accumulates into).
+ *
+ * Replaces: _broadcast_density_numba_parallel (solver_numba_parallel.py:222-277),
+ * _lax_wendroff_step_numba(_parallel) (solver_numba.py:130-213,
+ * solver_numba_parallel.py:280-418), apply_lateral_boundary /
+ * carry_lateral_ring and the swap (state.py:113-176,
+ * solver_numba_parallel.py:686-695), _sweep_kernel + _broadcast_kernel + the
+ * masked injected sum (solver_cuda.py:176-289, :325-354, :812).
+ */
+int pic_step(const pic_grid *g, const void *pos_in, const void *neg_in, void *pos_out, void *neg_out,
+             const void *dens, void *dens_zero, double *tally, void *workspace, int64_t workspace_bytes,
+             uintptr_t stream);
+
+/*
+ * pic_run_segment -- n_steps consecutive time steps on the device.
+ *
+ * Step s (0-based within the segment) reads fields[(parity + s) & 1] and
+ * writes fields[(parity + s + 1) & 1], where fields[b] = (pos_b, neg_b).
+ * Its tracks are xs/ys[track_offsets[s] .. track_offsets[s+1]) (host array of
+ * n_steps + 1 offsets into the device track arrays). Tallies go to
+ * tally[4*s .. 4*s+3] (device). dens0/dens1 alternate as the density buffer;
+ * both must be zero on the first call of a run.
+ *
+ * Replaces the per-step loop of run_simulation_numba_parallel /
+ * run_simulation_cuda (solver_numba_parallel.py:600-707,
+ * solver_cuda.py:791-872), without the per-step host synchronisation.
+ */
+int pic_run_segment(const pic_grid *g, void *pos0, void *neg0, void *pos1, void *neg1, int64_t parity,
+                    int64_t n_steps, const double *xs, const double *ys, const int64_t *track_offsets,
+                    void *dens0, void *dens1, int64_t dens_parity, uint32_t *counts, double *tally,
+                    void *workspace, int64_t workspace_bytes, uintptr_t stream);
+
+/*
+ * CUDA-graph form of pic_run_segment: the same launches captured once and
+ * replayed. The graph bakes in every pointer and the track offsets, so a
+ * replay is only valid with the same buffers; pic_graph_launch replays it on
+ * a stream. Used to replay a pulse's step sequence (every pulse has the same
+ * per-step track counts) and fixed-length idle segments.
+ */
+int pic_graph_create(const pic_grid *g, void *pos0, void *neg0, void *pos1, void *neg1, int64_t parity,
+                     int64_t n_steps, const double *xs, const double *ys, const int64_t *track_offsets,
+                     void *dens0, void *dens1, int64_t dens_parity, uint32_t *counts, double *tally,
+                     void *workspace, int64_t workspace_bytes, uintptr_t stream, uintptr_t *graph_out);
+int pic_graph_launch(uintptr_t graph, uintptr_t stream);
+int pic_graph_destroy(uintptr_t graph);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PIC_GB300_H */

@@ -1,0 +1,84 @@
+// deposit.cu -- one step's Gaussian ion tracks summed into the 2D density.
+//
+// A track is a line through the whole gap at constant LET, so its density is
+// the same in every gap layer: only the (i, j) cross-section is accumulated
+// here, and the fused step adds gaussian_factor * dens[i][j] to each gap layer
+// as it reads the fields. The cross-section is separable,
+//   exp(-((i-x)^2 + (j-y)^2) h^2/b^2) = g_i * g_j,
+// so a track costs one exponential per stencil row and column and one multiply
+// per cell (the identities of solver_numba.py:10-26). The stencil box is
+// [ceil(x - cut), floor(x + cut)] clipped to [0, no_xy), as in
+// solver_numba.py:86-89.
+//
+// One warp per track. Lanes own stencil columns j; row factors are computed
+// 32 rows at a time, one row per lane, and broadcast by shuffle. Each cell is
+// added with a float atomic: tracks overlap, and the L2 resolves the
+// collisions. The offset (i - x) is formed in float64 from the float64 track
+// centre before it is rounded, so the Gaussian is not shifted by the float32
+// spacing of x (up to 6e-5 voxel at x ~ 1000).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "pic_device.cuh"
+#include "pic_internal.h"
+
+namespace pic {
+
+__device__ __forceinline__ float gauss1(double d, float h2b2) {
+    const float f = (float)d;
+    return expf(-(f * f) * h2b2);
+}
+__device__ __forceinline__ double gauss1(double d, double h2b2) { return exp(-(d * d) * h2b2); }
+
+template <typename T, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) deposit_kernel(const double *__restrict__ xs,
+                                                              const double *__restrict__ ys, int64_t m,
+                                                              T *__restrict__ dens, uint32_t *__restrict__ counts,
+                                                              int64_t n, double cut, T h2b2) {
+    const int lane = threadIdx.x & 31;
+    const int64_t t = (int64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
+    if (t >= m) return;
+    const double x = xs[t], y = ys[t];
+    int64_t i_lo = (int64_t)ceil(x - cut), i_hi = (int64_t)floor(x + cut) + 1;
+    int64_t j_lo = (int64_t)ceil(y - cut), j_hi = (int64_t)floor(y + cut) + 1;
+    i_lo = i_lo < 0 ? 0 : i_lo;
+    j_lo = j_lo < 0 ? 0 : j_lo;
+    i_hi = i_hi > n ? n : i_hi;
+    j_hi = j_hi > n ? n : j_hi;
+    if (lane == 0) {
+        // int(x) floors for x >= 0; centres lie in [0, no_xy).
+        int64_t ix = (int64_t)x, iy = (int64_t)y;
+        if (ix >= 0 && ix < n && iy >= 0 && iy < n) atomicAdd(counts + ix * n + iy, 1u);
+    }
+    for (int64_t jb = j_lo; jb < j_hi; jb += 32) {
+        const int64_t j = jb + lane;
+        const bool jok = j < j_hi;
+        const T gj = jok ? gauss1((double)j - y, h2b2) : T(0);
+        for (int64_t ib = i_lo; ib < i_hi; ib += 32) {
+            const int rows = (int)((i_hi - ib) < 32 ? (i_hi - ib) : 32);
+            const T gi_lane = lane < rows ? gauss1((double)(ib + lane) - x, h2b2) : T(0);
+            for (int r = 0; r < rows; ++r) {
+                const T gi = __shfl_sync(0xffffffffu, gi_lane, r);
+                if (jok) atomicAdd(dens + (ib + r) * n + j, gi * gj);
+            }
+        }
+    }
+}
+
+int launch_deposit(const pic_grid *g, const double *xs, const double *ys, int64_t m, void *dens, uint32_t *counts,
+                   cudaStream_t st) {
+    if (m <= 0) return PIC_OK;
+    constexpr int WARPS = 8;
+    const int64_t blocks = (m + WARPS - 1) / WARPS;
+    if (g->dtype == PIC_F64) {
+        deposit_kernel<double, WARPS><<<(unsigned)blocks, WARPS * 32, 0, st>>>(
+            xs, ys, m, (double *)dens, counts, g->no_xy, g->cutoff_voxels, g->h2_over_b2);
+    } else {
+        deposit_kernel<float, WARPS><<<(unsigned)blocks, WARPS * 32, 0, st>>>(
+            xs, ys, m, (float *)dens, counts, g->no_xy, g->cutoff_voxels, (float)g->h2_over_b2);
+    }
+    return check_launch("deposit_kernel");
+}
+
+}  // namespace pic

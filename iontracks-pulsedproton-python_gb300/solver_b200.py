@@ -1,0 +1,143 @@
+"""``run_simulation_b200`` -- the GB300 backend behind the reference's
+solver signature.
+
+Same arguments and same :class:`Result` as the reference's drivers
+(``run_simulation_numba``, pulsed_ion_chamber/solver_numba.py:237-370, and the
+CUDA backend's ``max_steps`` / ``return_fields``, solver_cuda.py:645-654), so
+it drops in beside them and under the reference's output writers.
+
+How a run is driven:
+
+* the schedule and the track centres are drawn on the host from the same
+  NumPy stream as the reference (identical tracks for the same seed); a whole
+  pulse is sampled in one call and uploaded in one copy;
+* each pulse is one segment of steps on the device (deposition + fused step
+  per time step), the clearance gaps are segments without deposition; the
+  library's host loop launches a segment's kernels back to back with no host
+  synchronisation inside it;
+* per-step tallies stay on the device and come back once, at the end, in
+  float64; f(t) and k_s are formed from them as the reference forms them from
+  its running totals.
+
+The fields are float32 (``dtype="float32"``, the production mode) or float64
+(the validation mode). There is no CPU fallback: without a GB300 the call
+raises.
+"""
+
+from __future__ import annotations
+
+from time import perf_counter
+from typing import Optional
+
+import numpy as np
+
+from .engine import ChamberEngine
+from .pulses import TrackSampler, build_track_schedule
+from .state import Diagnostics, collection_efficiency
+
+
+def _segments(config, last_step: int):
+    """Consecutive (start, stop, with_tracks) segments covering [0, last_step)."""
+    segs = []
+    period = int(config.pulse_period_steps)
+    pulse = int(config.pulse_time_steps)
+    pos = 0
+    for p in range(int(config.n_pulses)):
+        s0 = p * period
+        s1 = min(s0 + pulse, last_step)
+        if s0 >= last_step:
+            break
+        if pos < s0:
+            segs.append((pos, s0, False))
+        segs.append((s0, s1, True))
+        pos = s1
+    if pos < last_step:
+        segs.append((pos, last_step, False))
+    return segs
+
+
+def run_simulation_b200(
+    config,
+    rng: Optional[np.random.Generator] = None,
+    progress: bool = True,
+    max_wall_s: Optional[float] = None,
+    max_steps: Optional[int] = None,
+    return_fields: bool = True,
+    dtype: str = "float32",
+    alpha_cm3_s: Optional[float] = None,
+    chunk_steps: int = 256,
+):
+    """Simulate a pulse train on one GB300 and return the reference's Result.
+
+    ``max_wall_s`` stops after the chunk in which that much wall time has
+    passed; ``max_steps`` after a fixed number of steps. Either sets
+    ``steps_completed`` and ``loop_elapsed_s`` on the Result and makes k_s
+    NaN when the run did not finish (pulsed_ion_chamber/solver_cuda.py:874-891).
+    ``return_fields=False`` returns empty field arrays. ``alpha_cm3_s``
+    overrides the recombination coefficient.
+    """
+    if dtype not in ("float32", "float64"):
+        raise ValueError(f"dtype must be 'float32' or 'float64', got {dtype!r}")
+    total = int(config.total_time_steps)
+    last_step = total if max_steps is None else max(0, min(total, int(max_steps)))
+    rng = rng if rng is not None else np.random.default_rng(config.seed)
+    schedule = build_track_schedule(config, rng)
+    sampler = TrackSampler(rng, config.mid_xy, config.sampling_radius, config.no_xy)
+    pulse_steps = int(config.pulse_time_steps)
+    max_pulse_tracks = int(schedule[:pulse_steps].sum())
+
+    eng = ChamberEngine(config, dtype=dtype, alpha_cm3_s=alpha_cm3_s, max_tracks=max_pulse_tracks)
+    torch = eng.torch
+    diagnostics = Diagnostics(config)
+    report_every = max(1, total // 20)
+    loop_t0 = perf_counter()
+    steps_done = 0
+    stopped = False
+
+    for s0, s1, with_tracks in _segments(config, last_step):
+        if with_tracks:
+            counts = schedule[s0:s1]
+            n = int(counts.sum())
+            xs, ys = sampler.sample(n)
+            eng.upload_tracks(xs, ys)
+            offsets = np.zeros(len(counts) + 1, dtype=np.int64)
+            np.cumsum(counts, out=offsets[1:])
+        else:
+            offsets = np.zeros(s1 - s0 + 1, dtype=np.int64)
+        # Chunks bound the wall-clock check and the progress report; the
+        # device never waits on the host inside a chunk.
+        c0 = 0
+        while c0 < s1 - s0:
+            c1 = min(c0 + chunk_steps, s1 - s0)
+            seg = offsets[c0 : c1 + 1] - offsets[c0]
+            eng.run_segment(seg, track_base=int(offsets[c0]))
+            steps_done = s0 + c1
+            if progress and (steps_done // report_every) != ((s0 + c0) // report_every):
+                print(f"  step {steps_done}/{total}")
+            if max_wall_s is not None:
+                torch.cuda.synchronize(eng.device)
+                if perf_counter() - loop_t0 >= max_wall_s:
+                    stopped = True
+                    break
+            c0 = c1
+        if stopped:
+            break
+
+    torch.cuda.synchronize(eng.device)
+    loop_elapsed_s = perf_counter() - loop_t0
+    tallies = eng.tallies(steps_done)
+    diagnostics.record_block(0, tallies)
+    diagnostics.track_density_xy = eng.track_density_xy()
+    f_t = collection_efficiency(diagnostics.injected, diagnostics.recombined, steps_done)
+    time_s = (np.arange(total) + 1) * config.dt
+    ks = float("nan") if steps_done < total else 1.0 / f_t[-1]
+    if return_fields:
+        pos, neg = eng.fields()
+    else:
+        pos, neg = np.zeros((0, 0, 0)), np.zeros((0, 0, 0))
+    result = diagnostics.build_result(config, time_s, f_t, ks, pos, neg)
+    if max_wall_s is not None or max_steps is not None:
+        result.steps_completed = steps_done
+        result.loop_elapsed_s = loop_elapsed_s
+    eng.close()
+    return result

@@ -88,10 +88,13 @@ def collection_efficiency(injected: np.ndarray, recombined: np.ndarray, steps_co
     :350): ``f = 1`` until something is injected, then ``(I - R) / I``. Steps
     past ``steps_completed`` keep 1.0, as in a run stopped early."""
     f_t = np.ones(len(injected))
-    total_i = 0.0
-    total_r = 0.0
-    for s in range(steps_completed):
-        total_i += injected[s]
-        total_r += recombined[s]
-        f_t[s] = 1.0 if total_i == 0.0 else (total_i - total_r) / total_i
+    n = int(steps_completed)
+    if n <= 0:
+        return f_t
+    # cumsum adds left to right, exactly the running float64 totals
+    total_i = np.cumsum(np.asarray(injected[:n], dtype=np.float64))
+    total_r = np.cumsum(np.asarray(recombined[:n], dtype=np.float64))
+    with np.errstate(invalid="ignore", divide="ignore"):
+        f = (total_i - total_r) / total_i
+    f_t[:n] = np.where(total_i == 0.0, 1.0, f)
     return f_t

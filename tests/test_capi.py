@@ -1,0 +1,102 @@
+"""The C-ABI library builds for sm_103a, loads without a GPU, and exports
+every entry point include/pic_gb300.h declares (no compute call here)."""
+
+import ctypes
+import re
+import subprocess
+from pathlib import Path
+
+import pytest
+
+from goldens import pkg
+
+ROOT = Path(__file__).resolve().parents[1]
+HEADER = ROOT / "include" / "pic_gb300.h"
+
+
+def _declared():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(pic_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import importlib
+
+    native = importlib.import_module(pkg().__name__ + "._native")
+    return native.load()
+
+
+def test_header_declares_the_entry_points():
+    names = _declared()
+    for must in ("pic_step", "pic_deposit", "pic_run_segment", "pic_last_error", "pic_graph_create"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in _declared():
+        assert hasattr(lib, name), name
+
+
+def test_exported_symbols_are_c_linkage():
+    import importlib
+
+    native = importlib.import_module(pkg().__name__ + "._native")
+    out = subprocess.run(["nm", "-D", "--defined-only", str(native.library_path())], capture_output=True, text=True)
+    syms = {line.split()[-1] for line in out.stdout.splitlines() if line.strip()}
+    for name in _declared():
+        assert name in syms, name
+
+
+def test_binding_covers_the_header(lib):
+    import importlib
+
+    native = importlib.import_module(pkg().__name__ + "._native")
+    assert set(_declared()) == set(native.EXPORTS)
+
+
+def test_host_only_calls_without_a_gpu(lib):
+    assert lib.pic_abi_version() == 1
+    assert lib.pic_kpitch(406) == 408
+    assert lib.pic_kpitch(408) == 408
+    assert lib.pic_kpitch(3) == 8
+
+
+def test_invalid_grid_is_refused_before_any_device_work(lib):
+    import importlib
+
+    native = importlib.import_module(pkg().__name__ + "._native")
+    g = native.PicGrid()
+    g.no_xy, g.nzb, g.kpitch, g.no_z, g.nze = 2, 10, 16, 4, 3
+    g.cutoff_voxels = 1.0
+    b = ctypes.c_int64()
+    rc = lib.pic_step_workspace_bytes(ctypes.byref(g), ctypes.byref(b))
+    assert rc == native.PIC_E_INVALID
+    assert b"no_xy" in lib.pic_last_error()
+    g.no_xy, g.kpitch = 8, 12
+    assert lib.pic_step_workspace_bytes(ctypes.byref(g), ctypes.byref(b)) == native.PIC_E_INVALID
+    assert b"kpitch" in lib.pic_last_error()
+    g.kpitch, g.nze = 16, 0
+    assert lib.pic_step_workspace_bytes(ctypes.byref(g), ctypes.byref(b)) == native.PIC_E_INVALID
+    g.nze = 3
+    assert lib.pic_step_workspace_bytes(ctypes.byref(g), ctypes.byref(b)) == native.PIC_OK
+    assert b.value > 0
+    rc = lib.pic_step(ctypes.byref(g), None, None, None, None, None, None, None, None, 0, None)
+    assert rc == native.PIC_E_INVALID
+
+
+def test_grid_descriptor_from_config():
+    import importlib
+
+    from goldens import make_config
+
+    eng = importlib.import_module(pkg().__name__ + ".engine")
+    cfg = make_config("column_10um_r008")
+    g = eng.make_grid(cfg)
+    assert (g.no_xy, g.nzb, g.kpitch, g.no_z, g.nze) == (24, 206, 208, 200, 3)
+    (pl, pzm, pzp, pc), _ = cfg.scheme_coefficients()
+    assert (g.p_lat, g.p_zm, g.p_zp, g.p_cen) == (pl, pzm, pzp, pc)
+    assert g.alpha_dt == 1.6e-6 * cfg.dt
+    with pytest.raises(ValueError):
+        eng.make_grid(cfg, dtype="float16")

@@ -1,0 +1,185 @@
+"""GPU parity: run_simulation_b200 against the reference's own outputs (golden
+fixtures) and against the FP64 oracle, through the C ABI on the GB300.
+
+Tolerances, per the project's parity bar:
+* track positions: identical (track_density_xy bit-equal);
+* float32 fields (production): |dk_s| <= 1e-5, cumulative injected and
+  recombined charge within 1e-5 relative, per-step tallies within 1e-5 of
+  their peak;
+* float64 fields (validation build): the same quantities within 1e-9
+  relative (the remaining difference is summation order and fused
+  multiply-adds).
+"""
+
+import importlib
+
+import numpy as np
+import pytest
+
+from goldens import available, make_config, pkg, run_config, run_fixture
+
+pytestmark = pytest.mark.gpu
+
+KS_ABS = 1e-5
+TALLY_REL = 1e-5
+F64_REL = 1e-9
+
+RUNS = [
+    "run_fast_base", "run_fast_reflecting", "run_fast_full_grid", "run_fast_two_species", "run_fast_nocutoff",
+    "run_fast_dense", "run_fast_dense_reflect_full", "run_small_absorbing", "run_small_reflecting",
+    "run_aic144_dev",
+]
+
+
+def _solver():
+    return pkg().run_simulation_b200
+
+
+def _check_f32(res, ks, injected, recombined, n_pos, n_neg, tracks):
+    np.testing.assert_array_equal(res.track_density_xy, tracks)
+    assert abs(res.ks - ks) <= KS_ABS, (res.ks, ks)
+    assert res.injected_positive.sum() == pytest.approx(injected.sum(), rel=TALLY_REL)
+    assert res.recombination.sum() == pytest.approx(recombined.sum(), rel=TALLY_REL)
+    for got, want in [(res.injected_positive, injected), (res.recombination, recombined),
+                      (res.n_positive, n_pos), (res.n_negative, n_neg)]:
+        peak = np.abs(want).max()
+        np.testing.assert_allclose(got, want, rtol=0, atol=TALLY_REL * peak)
+
+
+@pytest.mark.parametrize("name", RUNS)
+def test_float32_run_matches_reference(name):
+    cfg, fx = run_config(name)
+    res = _solver()(cfg, progress=False)
+    _check_f32(res, float(fx["ks"]), fx["injected"], fx["recombination"], fx["n_positive"], fx["n_negative"],
+               fx["track_density_xy"])
+    if "positive_array" in fx:
+        peak = np.abs(fx["positive_array"]).max()
+        np.testing.assert_allclose(res.positive_array, fx["positive_array"], rtol=0, atol=peak * 1e-5)
+        np.testing.assert_allclose(res.negative_array, fx["negative_array"], rtol=0, atol=peak * 1e-5)
+
+
+@pytest.mark.parametrize("name", RUNS)
+def test_float64_run_matches_reference(name):
+    cfg, fx = run_config(name)
+    res = _solver()(cfg, progress=False, dtype="float64")
+    np.testing.assert_array_equal(res.track_density_xy, fx["track_density_xy"])
+    assert res.ks == pytest.approx(float(fx["ks"]), rel=F64_REL)
+    for got, key in [(res.injected_positive, "injected"), (res.recombination, "recombination"),
+                     (res.n_positive, "n_positive"), (res.n_negative, "n_negative")]:
+        peak = np.abs(fx[key]).max()
+        np.testing.assert_allclose(got, fx[key], rtol=F64_REL, atol=F64_REL * peak, err_msg=key)
+    if "positive_array" in fx:
+        peak = np.abs(fx["positive_array"]).max()
+        np.testing.assert_allclose(res.positive_array, fx["positive_array"], rtol=0, atol=peak * F64_REL)
+        np.testing.assert_allclose(res.negative_array, fx["negative_array"], rtol=0, atol=peak * F64_REL)
+
+
+def test_plain_method_column_whole_run():
+    """24 x 24 x 206 at 10 um, r = 0.008 cm, seed 1: 1 622 steps, 22 837 tracks."""
+    name = "run_column_10um_r008"
+    if not available(name):
+        pytest.skip("fixture not generated")
+    cfg, fx = run_config(name)
+    res = _solver()(cfg, progress=False, return_fields=False)
+    _check_f32(res, float(fx["ks"]), fx["injected"], fx["recombination"], fx["n_positive"], fx["n_negative"],
+               fx["track_density_xy"])
+
+
+def test_published_dev_tier_k_s():
+    """The reference CLI's dev tier: k_s = 1.0580 (tests/test_examples_cli.py:24-53)."""
+    cfg, fx = run_config("run_aic144_dev")
+    res = _solver()(cfg, progress=False, return_fields=False)
+    assert res.ks == pytest.approx(1.0580, abs=1e-4)
+
+
+def test_fields_mid_run_match_the_oracle(oracle):
+    """The whole field, not only its tallies, at a step inside the pulse of a
+    grid with many tracks per step (fields and tallies in float64 mode)."""
+    cfg = make_config("rf_odd_noxy")  # odd no_xy: float centre
+    k = 120
+    ref = oracle.run(cfg, mode="batched", threads=4, max_steps=k + 1)
+    res = _solver()(cfg, progress=False, max_steps=k + 1, dtype="float64")
+    peak = np.abs(ref["positive"]).max()
+    np.testing.assert_allclose(res.positive_array, ref["positive"], rtol=0, atol=peak * F64_REL)
+    np.testing.assert_allclose(res.negative_array, ref["negative"], rtol=0, atol=peak * F64_REL)
+    res32 = _solver()(cfg, progress=False, max_steps=k + 1)
+    np.testing.assert_allclose(res32.positive_array, ref["positive"], rtol=0, atol=peak * 1e-5)
+
+
+def test_max_steps_truncates_and_reports():
+    cfg, _ = run_config("run_fast_dense")
+    full = _solver()(cfg, progress=False)
+    part = _solver()(cfg, progress=False, max_steps=5)
+    assert part.steps_completed == 5
+    assert part.loop_elapsed_s > 0
+    assert np.isnan(part.ks)
+    # float32 density sums use atomics, so two runs agree to float32
+    # rounding, not bit for bit
+    np.testing.assert_allclose(part.f_t[:5], full.f_t[:5], rtol=1e-7)
+
+
+def test_max_wall_s_stops_and_reports():
+    cfg, _ = run_config("run_fast_dense")
+    res = _solver()(cfg, progress=False, max_wall_s=0.0, chunk_steps=4)
+    assert res.steps_completed == 4
+    assert np.isnan(res.ks)
+
+
+def test_return_fields_false_drops_only_the_snapshot():
+    cfg, _ = run_config("run_fast_dense")
+    full = _solver()(cfg, progress=False)
+    lean = _solver()(cfg, progress=False, return_fields=False)
+    assert lean.positive_array.size == 0 and lean.negative_array.size == 0
+    assert lean.ks == pytest.approx(full.ks, rel=1e-6)
+
+
+def test_rejects_bad_dtype():
+    cfg, _ = run_config("run_fast_base")
+    with pytest.raises(ValueError, match="dtype"):
+        _solver()(cfg, progress=False, dtype="float16")
+
+
+def test_multi_pulse_run_against_the_oracle(oracle):
+    """Three pulses with idle gaps between them: the pulse/idle segmenting and
+    the density-buffer parity across segments."""
+    cfg = make_config("fast_dense", n_pulses=3, repetition_rate_hz=20000.0)
+    assert cfg.pulse_period_steps > cfg.pulse_time_steps
+    ref = oracle.run(cfg, mode="batched", threads=2)
+    res = _solver()(cfg, progress=False, chunk_steps=7)
+    np.testing.assert_array_equal(res.track_density_xy, ref["track_density_xy"])
+    assert abs(res.ks - ref["ks"]) <= KS_ABS
+    res64 = _solver()(cfg, progress=False, dtype="float64", chunk_steps=5)
+    assert res64.ks == pytest.approx(ref["ks"], rel=F64_REL)
+    np.testing.assert_allclose(res64.recombination, ref["recombined"], rtol=F64_REL,
+                               atol=F64_REL * np.abs(ref["recombined"]).max())
+
+
+@pytest.mark.parametrize("name", ["step_small_track_disc", "step_small_full_grid", "step_small_two_species"])
+def test_kernel_level_deposit_and_step(name):
+    """pic_deposit + pic_step through the C ABI on the reference's single-step
+    fixture (tests/test_charge_conservation.py): injected, recombined and the
+    carrier totals, and the stepped fields."""
+    import torch
+
+    eng_mod = importlib.import_module(pkg().__name__ + ".engine")
+    N = importlib.import_module(pkg().__name__ + "._native")
+    cfg, fx = run_config(name)
+    for dtype, tol in (("float64", 1e-12), ("float32", 1e-5)):
+        eng = eng_mod.ChamberEngine(cfg, dtype=dtype, max_tracks=len(fx["xs"]))
+        eng.upload_tracks(fx["xs"], fx["ys"], non_blocking=False)
+        eng.run_segment(np.array([0, len(fx["xs"])]))
+        torch.cuda.synchronize()
+        t = eng.tallies(1)[0]
+        assert t[0] == pytest.approx(float(fx["inserted"]), rel=tol)
+        assert t[1] == pytest.approx(float(fx["recombined"]), rel=tol)
+        assert t[2] == pytest.approx(float(fx["total_positive"]), rel=tol)
+        assert t[3] == pytest.approx(float(fx["total_negative"]), rel=tol)
+        pos, neg = eng.fields()
+        ref_pos = fx["positive_next"].copy()
+        peak = np.abs(fx["positive"]).max()
+        inner = (slice(1, -1), slice(1, -1), slice(None))
+        np.testing.assert_allclose(pos[inner], ref_pos[inner], rtol=0, atol=peak * tol)
+        np.testing.assert_allclose(neg[inner], fx["negative_next"][inner], rtol=0, atol=peak * tol)
+        dens = eng.dens[0].cpu().numpy().astype(np.float64)
+        np.testing.assert_allclose(dens, fx["total_density"], rtol=tol, atol=tol * fx["total_density"].max())
+        eng.close()
