@@ -140,6 +140,15 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def _shape(args):
+    shape = {"variant": args.variant}
+    for key in ("tile_rows", "planes_per_item", "stages", "consumer_warps", "ctas_per_sm"):
+        v = getattr(args, key)
+        if v:
+            shape[key] = v
+    return shape
+
+
 def _config(workload):
     desc, kw = WORKLOADS[workload]
     return desc, _pkg().SimulationConfig(**kw)
@@ -170,8 +179,6 @@ def run_reference(args):
     steps = max(1, args.ref_steps)
     vals = []
     cores = None
-    for _ in range(args.warmup if args.warmup < 1 else 0):
-        pass
     v, cores, wall = cpu_sample(cfg, steps=steps)
     vals.append(v)
     line = {
@@ -207,7 +214,9 @@ def run_gb300(args):
         raise SystemExit("warmup + steps must fit in the first pulse")
     counts = sched[:n_steps]
     xs, ys = pkg.TrackSampler(rng, cfg.mid_xy, cfg.sampling_radius, cfg.no_xy).sample(int(counts.sum()))
-    eng = eng_mod.ChamberEngine(cfg, dtype=args.dtype, max_tracks=len(xs), tally_steps=n_steps)
+    shape = _shape(args)
+    eng = eng_mod.ChamberEngine(cfg, dtype=args.dtype, max_tracks=len(xs), tally_steps=n_steps, shape=shape)
+    resolved = eng_mod.resolve_shape(eng.grid)
     eng.upload_tracks(xs, ys, non_blocking=False)
     off = np.zeros(n_steps + 1, dtype=np.int64)
     np.cumsum(counts, out=off[1:])
@@ -270,7 +279,7 @@ def run_gb300(args):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         res = pkg.run_simulation_b200(cfg, rng=np.random.default_rng(cfg.seed + rank), progress=False,
-                                      max_steps=args.e2e_steps, return_fields=False)
+                                      max_steps=args.e2e_steps, return_fields=False, shape=shape)
         torch.cuda.synchronize()
         e2e_s = time.perf_counter() - t0
         tracks = float(sched[: args.e2e_steps].sum())
@@ -295,10 +304,11 @@ def run_gb300(args):
                        "interior_voxels": vox, "tracks_in_timed_steps": int(counts[args.warmup:].sum()),
                        "l2": "fields 7.4 GB >> 129 MB L2: every step streams from HBM, no flush needed"
                        if args.workload == "full_electrode_5um" else "inputs smaller than L2",
-                       "parallelism": f"replicas x{world}"},
+                       "parallelism": f"replicas x{world}", "launch_shape": resolved},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
-                         "kernel": "step_kernel", "kernel_ms": step_ms,
+                         "kernel": "stream_step_kernel" if resolved["variant"] == "stream" else "step_kernel",
+                         "kernel_ms": step_ms,
                          "algorithmic_bytes_per_launch": BYTES_PER_VOXEL_STEP * vox},
             "cpu_baseline": cpu,
             "e2e": e2e,
@@ -322,6 +332,12 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=600)
     ap.add_argument("--ref-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--variant", choices=["auto", "flat", "stream"], default="auto")
+    ap.add_argument("--tile-rows", dest="tile_rows", type=int, default=0)
+    ap.add_argument("--planes-per-item", dest="planes_per_item", type=int, default=0)
+    ap.add_argument("--stages", type=int, default=0)
+    ap.add_argument("--consumer-warps", dest="consumer_warps", type=int, default=0)
+    ap.add_argument("--ctas-per-sm", dest="ctas_per_sm", type=int, default=0)
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")

@@ -58,12 +58,27 @@ typedef struct pic_grid {
     double cutoff_voxels;   /* deposition half-width                         */
     int32_t wall;           /* PIC_WALL_*                                    */
     int32_t dtype;          /* PIC_F32 or PIC_F64                            */
+    /* Launch shape of the fused step (0 = chosen by the library). */
+    int32_t variant;         /* PIC_VARIANT_*                                */
+    int32_t tile_rows;       /* stream variant: interior j rows per tile     */
+    int32_t planes_per_item; /* stream variant: i planes per work item       */
+    int32_t stages;          /* stream variant: shared-memory ring stages    */
+    int32_t consumer_warps;  /* stream variant: compute warps per CTA        */
+    int32_t ctas_per_sm;     /* stream variant: resident CTAs per SM         */
 } pic_grid;
+
+/* Fused-step kernels. FLAT: one thread per four k of a column, neighbours
+ * through L1/L2, any grid and either field type. STREAM: float32 only; whole
+ * (j-tile x k-row) planes staged in shared memory by bulk asynchronous copies
+ * while the CTA marches along i, for grids with no_xy >= 16. AUTO picks. */
+#define PIC_VARIANT_AUTO 0
+#define PIC_VARIANT_FLAT 1
+#define PIC_VARIANT_STREAM 2
 
 /* Description of the last failure on this host thread ("" if none). */
 const char *pic_last_error(void);
 
-/* ABI version (bumped on any signature change). */
+/* ABI version (bumped on any signature or struct change). */
 int pic_abi_version(void);
 
 /* k pitch for a given no_z_with_buffer: nzb rounded up to 8 elements. */
@@ -74,9 +89,19 @@ int64_t pic_kpitch(int64_t nzb);
 int pic_device_info(int32_t *sm_count, int64_t *total_bytes, int32_t *cc_major, int32_t *cc_minor);
 
 /* Bytes of device scratch the fused step needs for this grid (per-block
- * tally partials and a completion counter). The caller allocates it once,
- * zero-filled, and passes it to pic_step / pic_run_segment. */
+ * tally partials, a completion counter and a status word). The caller
+ * allocates it once, zero-filled, and passes it to pic_step /
+ * pic_run_segment. */
 int pic_step_workspace_bytes(const pic_grid *g, int64_t *bytes);
+
+/* Reads (and with reset != 0 clears) the status word a kernel sets in the
+ * workspace when a bounded wait gave up: 0 = ok, > 0 = the wait that
+ * expired. Synchronises the stream first. */
+int pic_workspace_status(void *workspace, int32_t reset, uintptr_t stream, int32_t *status);
+
+/* The launch shape the library would use for this grid when the shape
+ * fields are 0: fills variant .. ctas_per_sm of *resolved. */
+int pic_resolve_shape(const pic_grid *g, pic_grid *resolved);
 
 /*
  * pic_deposit -- sum one step's track Gaussians into the 2D density.

@@ -20,6 +20,9 @@ PIC_F32 = 0
 PIC_F64 = 1
 PIC_WALL_ABSORBING = 0
 PIC_WALL_REFLECTING = 1
+PIC_VARIANT_AUTO = 0
+PIC_VARIANT_FLAT = 1
+PIC_VARIANT_STREAM = 2
 
 _LIB_PATH = Path(__file__).resolve().parent / "_build" / "libpic_gb300.so"
 _lock = threading.Lock()
@@ -51,6 +54,12 @@ class PicGrid(ctypes.Structure):
         ("cutoff_voxels", ctypes.c_double),
         ("wall", ctypes.c_int32),
         ("dtype", ctypes.c_int32),
+        ("variant", ctypes.c_int32),
+        ("tile_rows", ctypes.c_int32),
+        ("planes_per_item", ctypes.c_int32),
+        ("stages", ctypes.c_int32),
+        ("consumer_warps", ctypes.c_int32),
+        ("ctas_per_sm", ctypes.c_int32),
     ]
 
 
@@ -65,6 +74,10 @@ EXPORTS = {
          ctypes.POINTER(ctypes.c_int32)],
     ),
     "pic_step_workspace_bytes": (ctypes.c_int, [ctypes.POINTER(PicGrid), ctypes.POINTER(ctypes.c_int64)]),
+    "pic_workspace_status": (
+        ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]
+    ),
+    "pic_resolve_shape": (ctypes.c_int, [ctypes.POINTER(PicGrid), ctypes.POINTER(PicGrid)]),
     "pic_deposit": (
         ctypes.c_int,
         [ctypes.POINTER(PicGrid), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,

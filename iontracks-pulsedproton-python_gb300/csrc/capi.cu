@@ -5,6 +5,7 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <cmath>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -47,6 +48,70 @@ int64_t step_grid_cap(int f64) {
     return c[dev];
 }
 
+int sm_count() {
+    static int cached[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    if (cached[dev] == 0) {
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cached[dev] = sms > 0 ? sms : 152;
+    }
+    return cached[dev];
+}
+
+int score_test(const pic_grid *g, ScoreTest *out) {
+    const double two_mid = 2.0 * g->mid_xy;
+    if (!(two_mid == std::floor(two_mid)) || two_mid < 0.0 || two_mid > 4.0 * (double)g->no_xy)
+        return set_error(PIC_E_INVALID, "mid_xy must be a multiple of 0.5 inside the grid (no_xy / 2)");
+    out->two_mid = (int64_t)two_mid;
+    const double r4 = 4.0 * g->scoring_radius_sq;  // exact: power-of-two scaling
+    const double cap = 4.0e18;
+    if (!(r4 > 0.0)) {
+        out->thr4 = -1;  // nothing is scored
+    } else if (r4 >= cap) {
+        out->thr4 = (int64_t)cap;
+    } else {
+        out->thr4 = (int64_t)std::ceil(r4) - 1;
+    }
+    return PIC_OK;
+}
+
+int resolve_shape(pic_grid *g) {
+    if (g->variant == PIC_VARIANT_AUTO)
+        g->variant = (g->dtype == PIC_F32 && g->no_xy >= 64) ? PIC_VARIANT_STREAM : PIC_VARIANT_FLAT;
+    if (g->variant == PIC_VARIANT_FLAT) return PIC_OK;
+    if (g->variant != PIC_VARIANT_STREAM) return set_error(PIC_E_INVALID, "variant must be PIC_VARIANT_AUTO, _FLAT or _STREAM");
+    if (g->dtype != PIC_F32) return set_error(PIC_E_INVALID, "the stream variant supports float32 fields only");
+    if (g->no_xy < 4) return set_error(PIC_E_INVALID, "the stream variant needs no_xy >= 4");
+    const int kp = (int)g->kpitch, c4 = kp / 4;
+    if (g->consumer_warps <= 0) g->consumer_warps = 16;
+    if (g->consumer_warps > kStreamMaxThreads / 32 - 1)
+        return set_error(PIC_E_INVALID, "consumer_warps must be <= " + std::to_string(kStreamMaxThreads / 32 - 1));
+    const int nct = g->consumer_warps * 32;
+    if (g->tile_rows <= 0) {
+        int tj = (2 * nct) / c4;
+        if (tj < 1) tj = 1;
+        if (tj > 16) tj = 16;
+        while (tj > 1 && 2 * (tj + 2) * kp * 4 > 48 * 1024) --tj;
+        g->tile_rows = tj;
+    }
+    if (g->tile_rows > (int)g->no_xy - 2) g->tile_rows = (int)g->no_xy - 2;
+    const int stage_bytes = (2 * (g->tile_rows + 2) * kp + ((g->tile_rows + 2 + 3) & ~3)) * 4;
+    // static shared memory of the kernel (reduction scratch, flags) is < 2 KB
+    const int budget = kStreamMaxSmem - 2048;
+    if (g->stages <= 0) {
+        int s = (budget - 128) / stage_bytes;
+        g->stages = s > 8 ? 8 : s;
+    }
+    if (g->stages < 4) return set_error(PIC_E_CAPACITY, "the stream variant needs 4 shared-memory stages for this k extent");
+    if (stream_smem_bytes(g->tile_rows, kp, g->stages) > budget)
+        return set_error(PIC_E_CAPACITY, "stream variant: tile_rows x stages exceed shared memory");
+    if (g->planes_per_item <= 0) g->planes_per_item = 64;
+    if (g->ctas_per_sm <= 0) g->ctas_per_sm = 1;
+    return PIC_OK;
+}
+
 static bool aligned(const void *p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
 
 static int check_grid(const pic_grid *g) {
@@ -63,7 +128,8 @@ static int check_grid(const pic_grid *g) {
     if (g->no_xy > (int64_t)1 << 20 || g->nzb > (int64_t)1 << 20)
         return set_error(PIC_E_CAPACITY, "grid extent beyond 2^20 voxels per axis");
     if (!(g->cutoff_voxels > 0.0)) return set_error(PIC_E_INVALID, "cutoff_voxels must be positive");
-    return PIC_OK;
+    ScoreTest t;
+    return score_test(g, &t);
 }
 
 static int check_fields(const void *a, const void *b, const void *c, const void *d) {
@@ -120,7 +186,7 @@ extern "C" {
 
 const char *pic_last_error(void) { return g_last_error.c_str(); }
 
-int pic_abi_version(void) { return 1; }
+int pic_abi_version(void) { return 2; }
 
 int64_t pic_kpitch(int64_t nzb) { return (nzb + 7) / 8 * 8; }
 
@@ -147,6 +213,31 @@ int pic_step_workspace_bytes(const pic_grid *g, int64_t *bytes) {
     if (!bytes) return set_error(PIC_E_INVALID, "bytes is null");
     *bytes = kWorkspaceBytes;
     return PIC_OK;
+}
+
+int pic_workspace_status(void *workspace, int32_t reset, uintptr_t stream, int32_t *status) {
+    if (!workspace || !status) return set_error(PIC_E_INVALID, "null pointer argument");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    Workspace w = workspace_layout(workspace);
+    int32_t v = 0;
+    cudaError_t e = cudaMemcpyAsync(&v, w.status, sizeof(v), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return set_cuda_error("pic_workspace_status", e);
+    *status = v;
+    if (reset && v != 0) {
+        e = cudaMemsetAsync(w.status, 0, sizeof(int32_t), st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return set_cuda_error("pic_workspace_status reset", e);
+    }
+    return PIC_OK;
+}
+
+int pic_resolve_shape(const pic_grid *g, pic_grid *resolved) {
+    int rc = check_grid(g);
+    if (rc) return rc;
+    if (!resolved) return set_error(PIC_E_INVALID, "resolved is null");
+    *resolved = *g;
+    return resolve_shape(resolved);
 }
 
 int pic_deposit(const pic_grid *g, const double *xs, const double *ys, int64_t n_tracks, void *dens,

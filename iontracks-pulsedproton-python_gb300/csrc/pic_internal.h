@@ -17,15 +17,50 @@ constexpr int64_t kMaxStepBlocks = 152 * 32;
 struct Workspace {
     double *partials;       // [kMaxStepBlocks][4]
     unsigned int *counter;  // completion counter, zero between steps
+    int *status;            // 0, or the code of a bounded wait that expired
 };
 
 inline Workspace workspace_layout(void *ws) {
     Workspace w;
-    w.partials = reinterpret_cast<double *>(ws);
-    w.counter = reinterpret_cast<unsigned int *>(reinterpret_cast<char *>(ws) + kMaxStepBlocks * 4 * sizeof(double));
+    char *base = reinterpret_cast<char *>(ws);
+    w.partials = reinterpret_cast<double *>(base);
+    w.counter = reinterpret_cast<unsigned int *>(base + kMaxStepBlocks * 4 * sizeof(double));
+    w.status = reinterpret_cast<int *>(base + kMaxStepBlocks * 4 * sizeof(double) + 128);
     return w;
 }
+
+// Largest CTA of the streaming step kernel: 16 consumer warps + 1 producer.
+constexpr int kStreamMaxThreads = 17 * 32;
+constexpr int kStreamMaxSmem = 227 * 1024;
+
+// Launch shape of the streaming step kernel.
+struct StreamShape {
+    int tile_rows, planes_per_item, stages, consumer_warps, ctas_per_sm, sm_count;
+};
+
+int stream_smem_bytes(int tj, int kp, int stages);
+int launch_stream_step(const pic_grid *g, const StreamShape &sh, const void *pos_in, const void *neg_in,
+                       void *pos_out, void *neg_out, const void *dens, void *dens_zero, double *tally, void *ws,
+                       cudaStream_t st);
+// Fills the shape fields of *g (variant .. ctas_per_sm) where they are 0.
+int resolve_shape(pic_grid *g);
 constexpr int64_t kWorkspaceBytes = kMaxStepBlocks * 4 * (int64_t)sizeof(double) + 256;
+
+// The scored-column test of the reference, (i - mid)^2 + (j - mid)^2 < r2
+// with mid = no_xy / 2 (pulsed_ion_chamber/config.py:254-255), in exact
+// integer form: with dx = 2 i - 2 mid and dy = 2 j - 2 mid (integers), the
+// float64 comparison is exact (half-integer squares are exact) and equals
+// dx^2 + dy^2 <= ceil(4 r2) - 1. Keeps float64 off the per-voxel path (the
+// GPU's FP64 rate is ~1/64 of its FP32 rate).
+struct ScoreTest {
+    int64_t two_mid;
+    int64_t thr4;
+};
+int score_test(const pic_grid *g, ScoreTest *out);
+__host__ __device__ inline bool scored_column(const ScoreTest &t, int64_t i, int64_t j) {
+    const int64_t dx = 2 * i - t.two_mid, dy = 2 * j - t.two_mid;
+    return dx * dx + dy * dy <= t.thr4;
+}
 
 int set_error(int code, const std::string &msg);
 int set_cuda_error(const char *what, cudaError_t e);
@@ -34,6 +69,7 @@ int check_launch(const char *what);
 // Largest useful grid for the step kernel on the current device (SMs x
 // resident blocks), cached per device.
 int64_t step_grid_cap(int f64);
+int sm_count();
 int step_occupancy(int dtype, int *blocks_per_sm);
 
 int launch_step(const pic_grid *g, const void *pos_in, const void *neg_in, void *pos_out, void *neg_out,

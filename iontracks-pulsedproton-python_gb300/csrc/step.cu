@@ -41,7 +41,8 @@ struct StepArgs {
     int nzb, nze, gap_end;  // gap = [nze, gap_end)
     int reflecting;
     T p_lat, p_zm, p_zp, p_cen, n_lat, n_zm, n_zp, n_cen, alpha_dt, gfac;
-    double mid, srsq, injected_scale;
+    ScoreTest score;
+    double injected_scale;
 };
 
 template <typename T>
@@ -117,8 +118,7 @@ __global__ void __launch_bounds__(BLOCK) step_kernel(StepArgs<T> a) {
             if (g_kp) { pkp += dc; nkp += dc; }
         }
 
-        double di_c = (double)ci - a.mid, dj_c = (double)cj - a.mid;
-        const bool scored_col = !ring && (di_c * di_c + dj_c * dj_c < a.srsq);
+        const bool scored_col = !ring && scored_column(a.score, ci, cj);
         V4<T> PO, NO;
         T rec_sum = 0, p_sum = 0, n_sum = 0;
 #pragma unroll
@@ -185,8 +185,8 @@ static int launch_step_t(const pic_grid *g, const void *pos_in, const void *neg_
     a.n_lat = (T)g->n_lat; a.n_zm = (T)g->n_zm; a.n_zp = (T)g->n_zp; a.n_cen = (T)g->n_cen;
     a.alpha_dt = (T)g->alpha_dt;
     a.gfac = (T)g->gaussian_factor;
-    a.mid = g->mid_xy;
-    a.srsq = g->scoring_radius_sq;
+    int rc = score_test(g, &a.score);
+    if (rc) return rc;
     a.injected_scale = g->gaussian_factor * (double)g->no_z;
     int64_t blocks = (a.items + BLOCK - 1) / BLOCK;
     const int64_t cap = step_grid_cap(g->dtype == PIC_F64 ? 1 : 0);
@@ -196,8 +196,16 @@ static int launch_step_t(const pic_grid *g, const void *pos_in, const void *neg_
     return check_launch("step_kernel");
 }
 
-int launch_step(const pic_grid *g, const void *pos_in, const void *neg_in, void *pos_out, void *neg_out,
+int launch_step(const pic_grid *g_in, const void *pos_in, const void *neg_in, void *pos_out, void *neg_out,
                 const void *dens, void *dens_zero, double *tally, void *ws, cudaStream_t st) {
+    pic_grid r = *g_in;
+    int rc = resolve_shape(&r);
+    if (rc) return rc;
+    const pic_grid *g = &r;
+    if (g->variant == PIC_VARIANT_STREAM) {
+        StreamShape sh{g->tile_rows, g->planes_per_item, g->stages, g->consumer_warps, g->ctas_per_sm, sm_count()};
+        return launch_stream_step(g, sh, pos_in, neg_in, pos_out, neg_out, dens, dens_zero, tally, ws, st);
+    }
     if (g->dtype == PIC_F64)
         return launch_step_t<double>(g, pos_in, neg_in, pos_out, neg_out, dens, dens_zero, tally, ws, st);
     return launch_step_t<float>(g, pos_in, neg_in, pos_out, neg_out, dens, dens_zero, tally, ws, st);

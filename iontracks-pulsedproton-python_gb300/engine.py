@@ -18,11 +18,37 @@ from . import _native as N
 from .constants import RECOMBINATION_ALPHA_CM3_S
 
 _DTYPES = {"float32": N.PIC_F32, "float64": N.PIC_F64}
+_VARIANTS = {"auto": N.PIC_VARIANT_AUTO, "flat": N.PIC_VARIANT_FLAT, "stream": N.PIC_VARIANT_STREAM}
+SHAPE_FIELDS = ("variant", "tile_rows", "planes_per_item", "stages", "consumer_warps", "ctas_per_sm")
 
 
-def make_grid(config, dtype: str = "float32", alpha_cm3_s: float | None = None) -> N.PicGrid:
+def apply_shape(g: N.PicGrid, shape: dict | None) -> N.PicGrid:
+    """Sets launch-shape fields of a descriptor from a dict (``variant`` may
+    be ``"auto"``, ``"flat"`` or ``"stream"``); unknown keys raise."""
+    for key, val in (shape or {}).items():
+        if key not in SHAPE_FIELDS:
+            raise ValueError(f"unknown launch-shape field {key!r}; expected one of {SHAPE_FIELDS}")
+        if key == "variant" and isinstance(val, str):
+            if val not in _VARIANTS:
+                raise ValueError(f"variant must be one of {sorted(_VARIANTS)}, got {val!r}")
+            val = _VARIANTS[val]
+        setattr(g, key, int(val))
+    return g
+
+
+def resolve_shape(g: N.PicGrid) -> dict:
+    """The launch shape the library will use for this descriptor."""
+    out = N.PicGrid()
+    N.check(N.load().pic_resolve_shape(ctypes.byref(g), ctypes.byref(out)), "pic_resolve_shape")
+    d = {k: int(getattr(out, k)) for k in SHAPE_FIELDS}
+    d["variant"] = {v: k for k, v in _VARIANTS.items()}[d["variant"]]
+    return d
+
+
+def make_grid(config, dtype: str = "float32", alpha_cm3_s: float | None = None, shape: dict | None = None) -> N.PicGrid:
     """The ``pic_grid`` descriptor of a configuration (any object with the
-    reference SimulationConfig's attributes)."""
+    reference SimulationConfig's attributes), with optional launch-shape
+    overrides."""
     if dtype not in _DTYPES:
         raise ValueError(f"dtype must be 'float32' or 'float64', got {dtype!r}")
     (p_lat, p_zm, p_zp, p_cen), (n_lat, n_zm, n_zp, n_cen) = config.scheme_coefficients()
@@ -43,7 +69,7 @@ def make_grid(config, dtype: str = "float32", alpha_cm3_s: float | None = None) 
     g.cutoff_voxels = float(config.track_cutoff_voxels)
     g.wall = N.PIC_WALL_REFLECTING if config.lateral_boundary == "reflecting" else N.PIC_WALL_ABSORBING
     g.dtype = _DTYPES[dtype]
-    return g
+    return apply_shape(g, shape)
 
 
 def device_bytes(config, dtype: str = "float32", max_tracks: int = 0) -> int:
@@ -58,7 +84,7 @@ class ChamberEngine:
     """HBM state of one run plus the entry points that advance it."""
 
     def __init__(self, config, dtype: str = "float32", alpha_cm3_s: float | None = None, max_tracks: int = 0,
-                 device=None, tally_steps: int | None = None):
+                 device=None, tally_steps: int | None = None, shape: dict | None = None):
         import torch
 
         if not torch.cuda.is_available():
@@ -69,7 +95,7 @@ class ChamberEngine:
         N.device_info()  # raises unless the current device is sm_103
         self.config = config
         self.dtype = dtype
-        self.grid = make_grid(config, dtype, alpha_cm3_s)
+        self.grid = make_grid(config, dtype, alpha_cm3_s, shape)
         need = device_bytes(config, dtype, max_tracks)
         free, _total = torch.cuda.mem_get_info(self.device)
         if need > 0.9 * free:
@@ -180,6 +206,15 @@ class ChamberEngine:
         N.check(self.lib.pic_graph_launch(handle, self._stream(stream)), "pic_graph_launch")
         self.parity = (self.parity + n_steps) & 1
         self.step_index += n_steps
+
+    def check_status(self, stream=None) -> None:
+        """Raises if a kernel's bounded wait expired since the last check
+        (the status word in the step workspace)."""
+        st = ctypes.c_int32()
+        N.check(self.lib.pic_workspace_status(self.workspace.data_ptr(), 1, self._stream(stream), ctypes.byref(st)),
+                "pic_workspace_status")
+        if st.value != 0:
+            raise RuntimeError(f"a fused-step kernel gave up on a bounded wait (code {st.value}); results are invalid")
 
     def close(self) -> None:
         for h, _ in self._graphs.values():

@@ -66,6 +66,7 @@ def run_simulation_b200(
     dtype: str = "float32",
     alpha_cm3_s: Optional[float] = None,
     chunk_steps: int = 256,
+    shape: Optional[dict] = None,
 ):
     """Simulate a pulse train on one GB300 and return the reference's Result.
 
@@ -74,7 +75,9 @@ def run_simulation_b200(
     ``steps_completed`` and ``loop_elapsed_s`` on the Result and makes k_s
     NaN when the run did not finish (pulsed_ion_chamber/solver_cuda.py:874-891).
     ``return_fields=False`` returns empty field arrays. ``alpha_cm3_s``
-    overrides the recombination coefficient.
+    overrides the recombination coefficient. ``shape`` overrides the fused
+    step's launch shape (``variant`` "flat"/"stream", ``tile_rows``, ...);
+    by default the library chooses.
     """
     if dtype not in ("float32", "float64"):
         raise ValueError(f"dtype must be 'float32' or 'float64', got {dtype!r}")
@@ -86,7 +89,7 @@ def run_simulation_b200(
     pulse_steps = int(config.pulse_time_steps)
     max_pulse_tracks = int(schedule[:pulse_steps].sum())
 
-    eng = ChamberEngine(config, dtype=dtype, alpha_cm3_s=alpha_cm3_s, max_tracks=max_pulse_tracks)
+    eng = ChamberEngine(config, dtype=dtype, alpha_cm3_s=alpha_cm3_s, max_tracks=max_pulse_tracks, shape=shape)
     torch = eng.torch
     diagnostics = Diagnostics(config)
     report_every = max(1, total // 20)
@@ -125,6 +128,7 @@ def run_simulation_b200(
 
     torch.cuda.synchronize(eng.device)
     loop_elapsed_s = perf_counter() - loop_t0
+    eng.check_status()
     tallies = eng.tallies(steps_done)
     diagnostics.record_block(0, tallies)
     diagnostics.track_density_xy = eng.track_density_xy()

@@ -57,7 +57,7 @@ def test_binding_covers_the_header(lib):
 
 
 def test_host_only_calls_without_a_gpu(lib):
-    assert lib.pic_abi_version() == 1
+    assert lib.pic_abi_version() == 2
     assert lib.pic_kpitch(406) == 408
     assert lib.pic_kpitch(408) == 408
     assert lib.pic_kpitch(3) == 8
@@ -100,3 +100,30 @@ def test_grid_descriptor_from_config():
     assert g.alpha_dt == 1.6e-6 * cfg.dt
     with pytest.raises(ValueError):
         eng.make_grid(cfg, dtype="float16")
+
+
+def test_launch_shape_resolution_without_a_gpu():
+    import importlib
+
+    from goldens import make_config
+
+    eng = importlib.import_module(pkg().__name__ + ".engine")
+    big = eng.make_grid(make_config("full_electrode_5um_10p"))
+    s = eng.resolve_shape(big)
+    assert s["variant"] == "stream"
+    assert s["tile_rows"] == 10 and s["stages"] == 5 and s["consumer_warps"] == 16
+    small = eng.make_grid(make_config("column_10um_r008"))
+    assert eng.resolve_shape(small)["variant"] == "flat"
+    f64 = eng.make_grid(make_config("full_electrode_5um_10p"), dtype="float64")
+    assert eng.resolve_shape(f64)["variant"] == "flat"
+    forced = eng.make_grid(make_config("fast"), shape={"variant": "stream", "tile_rows": 3, "stages": 4})
+    s = eng.resolve_shape(forced)
+    assert (s["variant"], s["tile_rows"], s["stages"]) == ("stream", 3, 4)
+    bad = eng.make_grid(make_config("fast"), dtype="float64", shape={"variant": "stream"})
+    with pytest.raises(RuntimeError, match="float32"):
+        eng.resolve_shape(bad)
+    with pytest.raises(ValueError, match="launch-shape"):
+        eng.make_grid(make_config("fast"), shape={"warps": 3})
+    wide = eng.make_grid(make_config("sweep_hi"), shape={"variant": "stream"})
+    s = eng.resolve_shape(wide)
+    assert s["stages"] >= 4

@@ -183,3 +183,57 @@ def test_kernel_level_deposit_and_step(name):
         dens = eng.dens[0].cpu().numpy().astype(np.float64)
         np.testing.assert_allclose(dens, fx["total_density"], rtol=tol, atol=tol * fx["total_density"].max())
         eng.close()
+
+
+STREAM_SHAPES = {
+    "tiny_tiles": dict(variant="stream", tile_rows=3, planes_per_item=5, stages=4, consumer_warps=2),
+    "mid": dict(variant="stream", tile_rows=7, planes_per_item=9, stages=6, consumer_warps=5),
+    "default": dict(variant="stream"),
+}
+STREAM_RUNS = ["run_fast_base", "run_fast_reflecting", "run_fast_full_grid", "run_fast_two_species",
+               "run_fast_dense", "run_fast_dense_reflect_full", "run_small_absorbing", "run_small_reflecting",
+               "run_aic144_dev"]
+
+
+@pytest.mark.parametrize("shape", sorted(STREAM_SHAPES))
+@pytest.mark.parametrize("name", STREAM_RUNS)
+def test_stream_variant_matches_reference(name, shape):
+    """The shared-memory streaming kernel, forced on small grids with several
+    tiles and work items per grid, against the reference fixtures."""
+    cfg, fx = run_config(name)
+    res = _solver()(cfg, progress=False, shape=STREAM_SHAPES[shape])
+    _check_f32(res, float(fx["ks"]), fx["injected"], fx["recombination"], fx["n_positive"], fx["n_negative"],
+               fx["track_density_xy"])
+    if "positive_array" in fx:
+        peak = np.abs(fx["positive_array"]).max()
+        np.testing.assert_allclose(res.positive_array, fx["positive_array"], rtol=0, atol=peak * 1e-5)
+        np.testing.assert_allclose(res.negative_array, fx["negative_array"], rtol=0, atol=peak * 1e-5)
+
+
+@pytest.mark.parametrize("wall", ["absorbing", "reflecting"])
+def test_stream_and_flat_agree_on_a_large_grid(wall):
+    """208 x 208 x 406 (5 um, r = 0.05 cm), 40 steps of the pulse at 89.1 Gy/s
+    (~3 000 tracks a step): the two kernels give the same fields and tallies
+    to float32 rounding."""
+    cfg = make_config("column_5um_r05_d89p1", lateral_boundary=wall)
+    a = _solver()(cfg, progress=False, max_steps=40, shape={"variant": "flat"})
+    b = _solver()(cfg, progress=False, max_steps=40, shape={"variant": "stream"})
+    np.testing.assert_array_equal(a.track_density_xy, b.track_density_xy)
+    for x, y in [(a.recombination, b.recombination), (a.n_positive, b.n_positive), (a.injected_positive,
+                                                                                     b.injected_positive)]:
+        np.testing.assert_allclose(x[:40], y[:40], rtol=2e-6, atol=0)
+    peak = np.abs(a.positive_array).max()
+    np.testing.assert_allclose(b.positive_array, a.positive_array, rtol=0, atol=peak * 2e-6)
+    np.testing.assert_allclose(b.negative_array, a.negative_array, rtol=0, atol=peak * 2e-6)
+
+
+def test_stream_fields_mid_run_match_the_oracle(oracle):
+    cfg = make_config("rf_odd_noxy", lateral_boundary="reflecting")
+    k = 90
+    ref = oracle.run(cfg, mode="batched", threads=4, max_steps=k + 1)
+    res = _solver()(cfg, progress=False, max_steps=k + 1, shape=dict(variant="stream", tile_rows=4,
+                                                                     planes_per_item=6))
+    peak = np.abs(ref["positive"]).max()
+    np.testing.assert_allclose(res.positive_array, ref["positive"], rtol=0, atol=peak * 1e-5)
+    np.testing.assert_allclose(res.negative_array, ref["negative"], rtol=0, atol=peak * 1e-5)
+    assert res.recombination[:k + 1].sum() == pytest.approx(ref["recombined"][:k + 1].sum(), rel=TALLY_REL)
