@@ -25,7 +25,6 @@ from . import _native as N
 from .engine import SHAPE_FIELDS, apply_shape, resolve_shape
 
 CACHE = Path(os.environ.get("PIC_TUNE_CACHE", Path(__file__).resolve().parent / "_build" / "tuning.json"))
-_REGS_PER_THREAD = 96  # streaming kernel, from ptxas
 _SMEM_PER_SM = 228 * 1024
 
 
@@ -35,16 +34,21 @@ def candidate_shapes(grid, quick: bool = False) -> list[dict]:
     if grid.dtype != N.PIC_F32 or grid.no_xy < 16:
         return out
     kp = grid.kpitch
-    tjs = (3, 5, 8, 10) if quick else (2, 3, 4, 5, 6, 8, 10, 12, 16)
-    cws = (8, 16) if quick else (4, 8, 12, 16)
+    tjs = (3, 5, 8, 10) if quick else (2, 3, 4, 5, 6, 8, 10, 12)
+    cws = (8, 12, 16) if quick else (4, 6, 8, 10, 12, 16)
     planes = (64,) if quick else (32, 64, 128)
-    for tj, cw, ctas, stages, li in itertools.product(tjs, cws, (1, 2, 3), (4, 5, 6, 8), planes):
+    stage_counts = (4, 6, 8) if quick else (4, 5, 6, 8, 10, 12, 16)
+    for tj, cw, ctas, stages, li in itertools.product(tjs, cws, (1, 2), stage_counts, planes):
         if tj > grid.no_xy - 2:
             continue
         smem = (2 * stages * 8 + 127) // 128 * 128 + stages * (2 * (tj + 2) * kp + ((tj + 5) & ~3)) * 4
         if ctas * (smem + 3 * 1024) > _SMEM_PER_SM:
             continue
-        if ctas * (cw + 1) * 32 * _REGS_PER_THREAD > 65536:
+        ipt = -(-(tj * (kp // 4)) // (cw * 32))
+        if ipt > 4 or (cw + 1) * 32 > (544, 416, 352, 288)[ipt - 1]:
+            continue
+        regs = (96, 128, 144, 160)[ipt - 1]
+        if ctas * (cw + 1) * 32 * regs > 65536:
             continue
         out.append(dict(variant="stream", tile_rows=tj, consumer_warps=cw, ctas_per_sm=ctas, stages=stages,
                         planes_per_item=li))

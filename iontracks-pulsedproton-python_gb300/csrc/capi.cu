@@ -67,9 +67,8 @@ int score_test(const pic_grid *g, ScoreTest *out) {
     out->two_mid = (int64_t)two_mid;
     const double r4 = 4.0 * g->scoring_radius_sq;  // exact: power-of-two scaling
     const double cap = 4.0e18;
-    if (!(r4 > 0.0)) {
-        out->thr4 = -1;  // nothing is scored
-    } else if (r4 >= cap) {
+    if (!(r4 > 0.0)) return set_error(PIC_E_INVALID, "scoring_radius_sq must be positive");
+    if (r4 >= cap) {
         out->thr4 = (int64_t)cap;
     } else {
         out->thr4 = (int64_t)std::ceil(r4) - 1;
@@ -85,7 +84,7 @@ int resolve_shape(pic_grid *g) {
     if (g->dtype != PIC_F32) return set_error(PIC_E_INVALID, "the stream variant supports float32 fields only");
     if (g->no_xy < 4) return set_error(PIC_E_INVALID, "the stream variant needs no_xy >= 4");
     const int kp = (int)g->kpitch, c4 = kp / 4;
-    if (g->consumer_warps <= 0) g->consumer_warps = 16;
+    if (g->consumer_warps <= 0) g->consumer_warps = 12;
     if (g->consumer_warps > kStreamMaxThreads / 32 - 1)
         return set_error(PIC_E_INVALID, "consumer_warps must be <= " + std::to_string(kStreamMaxThreads / 32 - 1));
     const int nct = g->consumer_warps * 32;
@@ -97,14 +96,24 @@ int resolve_shape(pic_grid *g) {
         g->tile_rows = tj;
     }
     if (g->tile_rows > (int)g->no_xy - 2) g->tile_rows = (int)g->no_xy - 2;
+    if (g->tile_rows * c4 > 4 * nct)
+        return set_error(PIC_E_INVALID, "stream variant: tile_rows * kpitch/4 must be <= 4 * 32 * consumer_warps");
+    {
+        const int ipt = (g->tile_rows * c4 + nct - 1) / nct;
+        if (nct + 32 > stream_max_threads(ipt))
+            return set_error(PIC_E_INVALID, "stream variant: " + std::to_string(g->consumer_warps) +
+                                                " consumer warps exceed the register budget of " +
+                                                std::to_string(ipt) + " items per thread");
+    }
     const int stage_bytes = (2 * (g->tile_rows + 2) * kp + ((g->tile_rows + 2 + 3) & ~3)) * 4;
     // static shared memory of the kernel (reduction scratch, flags) is < 2 KB
     const int budget = kStreamMaxSmem - 2048;
     if (g->stages <= 0) {
-        int s = (budget - 128) / stage_bytes;
-        g->stages = s > 8 ? 8 : s;
+        int s = (budget - 256) / stage_bytes;
+        g->stages = s > 16 ? 16 : s;
     }
     if (g->stages < 4) return set_error(PIC_E_CAPACITY, "the stream variant needs 4 shared-memory stages for this k extent");
+    if (g->stages > 16) return set_error(PIC_E_INVALID, "stream variant: at most 16 stages");
     if (stream_smem_bytes(g->tile_rows, kp, g->stages) > budget)
         return set_error(PIC_E_CAPACITY, "stream variant: tile_rows x stages exceed shared memory");
     if (g->planes_per_item <= 0) g->planes_per_item = 64;

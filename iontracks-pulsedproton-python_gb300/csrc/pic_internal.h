@@ -31,6 +31,12 @@ inline Workspace workspace_layout(void *ws) {
 
 // Largest CTA of the streaming step kernel: 16 consumer warps + 1 producer.
 constexpr int kStreamMaxThreads = 17 * 32;
+// Block-size bound of the streaming kernel instantiated for IPT items per
+// consumer thread; a smaller bound leaves each thread more registers, so the
+// IPT items of a plane can be unrolled without spilling.
+__host__ __device__ constexpr int stream_max_threads(int ipt) {
+    return ipt <= 1 ? 17 * 32 : (ipt == 2 ? 13 * 32 : (ipt == 3 ? 11 * 32 : 9 * 32));
+}
 constexpr int kStreamMaxSmem = 227 * 1024;
 
 // Launch shape of the streaming step kernel.

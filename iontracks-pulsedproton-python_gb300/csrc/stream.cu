@@ -41,7 +41,8 @@ struct StreamArgs {
     int n, kp, c4, nzb, nze, gap_end, reflecting;
     int tj, li, jt, n_items, stages, consumer_warps;
     float p_lat, p_zm, p_zp, p_cen, n_lat, n_zm, n_zp, n_cen, alpha_dt, gfac;
-    ScoreTest score;
+    int two_mid;    // 2 * mid_xy
+    uint32_t thr4;  // scored iff (2i - two_mid)^2 + (2j - two_mid)^2 <= thr4
     double injected_scale;
 };
 
@@ -55,13 +56,6 @@ __device__ __forceinline__ void item_geometry(const StreamArgs &a, int w, int &c
 }
 
 __device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
-
-__device__ __forceinline__ void add_dep(float4 &v, float d, const bool (&g)[4]) {
-    v.x += g[0] ? d : 0.f;
-    v.y += g[1] ? d : 0.f;
-    v.z += g[2] ? d : 0.f;
-    v.w += g[3] ? d : 0.f;
-}
 
 __device__ __forceinline__ void st4(float *p, float4 v) { *reinterpret_cast<float4 *>(p) = v; }
 
@@ -108,7 +102,8 @@ __device__ void finish_tally_rt(double (&v)[4], double *partials, unsigned int *
     }
 }
 
-__global__ void __launch_bounds__(kStreamMaxThreads, 1) stream_step_kernel(StreamArgs a) {
+template <int IPT>
+__global__ void __launch_bounds__(stream_max_threads(IPT), 1) stream_step_kernel(StreamArgs a) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ volatile int abort_flag;
     uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw);
@@ -176,19 +171,64 @@ __global__ void __launch_bounds__(kStreamMaxThreads, 1) stream_step_kernel(Strea
         }
     } else {
         // ---------------- consumers ----------------
+        // The k-vectors of a row split into CORE vectors, whose four elements
+        // all lie in the gap (always valid, always deposited into, scored when
+        // the column is), and EDGE vectors (the k = 0 plane, the electrode
+        // buffers, the z end plane and the row padding). Core vectors take a
+        // mask-free path in packed FP32x2 arithmetic; edge vectors the general
+        // masked one. Work slot s of a plane is core item s (row s / ncore,
+        // vector c_lo + s % ncore) for s < n_core, then edge items; consumer
+        // thread t owns slots t + k * nct, k < IPT, so consecutive lanes hold
+        // consecutive core vectors of a row and trade their edge elements (the
+        // k-1 / k+4 neighbours) by shuffle.
         const int ctid = threadIdx.x;
         const int nct = cw * 32;
-        const int n = a.n, kp = a.kp;
+        const int n = a.n, kp = a.kp, c4 = a.c4;
+        const int c_lo = (a.nze + 3) / 4, c_hi = a.gap_end / 4;  // core vectors: [c_lo, c_hi)
+        const int ncore = c_hi > c_lo ? c_hi - c_lo : 0;
+        const int nedge = c4 - ncore;
+        const bool gap_below = 4 * c_lo - 1 >= a.nze;  // element before the first core vector
+        const bool gap_above = 4 * c_hi < a.gap_end;   // element after the last core vector
+        const int64_t plane_stride = (int64_t)n * kp;
+        const float2 ZMp = make_float2(a.p_zm, a.p_zm), ZPp = make_float2(a.p_zp, a.p_zp);
+        const float2 LATp = make_float2(a.p_lat, a.p_lat), CENp = make_float2(a.p_cen, a.p_cen);
+        const float2 ZMn = make_float2(a.n_zm, a.n_zm), ZPn = make_float2(a.n_zp, a.n_zp);
+        const float2 LATn = make_float2(a.n_lat, a.n_lat), CENn = make_float2(a.n_cen, a.n_cen);
+        const float2 ADT = make_float2(a.alpha_dt, a.alpha_dt), NEG1 = make_float2(-1.f, -1.f);
         long long g = 0;
         for (int w = blockIdx.x; w < a.n_items; w += gridDim.x) {
             int cj_lo, cj_hi, ci_lo, ci_hi;
             item_geometry(a, w, cj_lo, cj_hi, ci_lo, ci_hi);
             const int nplanes = ci_hi - ci_lo + 2;
+            const int rows_out = cj_hi - cj_lo;
+            const int n_core = rows_out * ncore, n_all = rows_out * c4;
+            // per-slot constants: kind (0 dead, 1 core, 2 edge), row+1, vector
+            int kind[IPT], rs_[IPT], c_[IPT];
+            uint32_t dy2[IPT];
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                const int sl = ctid + k * nct;
+                int r = 0, c = 0, kd = 0;
+                if (sl < n_core) {
+                    r = sl / ncore;
+                    c = c_lo + (sl - r * ncore);
+                    kd = 1;
+                } else if (sl < n_all) {
+                    const int e = sl - n_core;
+                    r = e / nedge;
+                    const int ei = e - r * nedge;
+                    c = ei < c_lo ? ei : ncore + ei;  // edge vectors below, then above the core
+                    kd = 2;
+                }
+                kind[k] = kd;
+                rs_[k] = r + 1;
+                c_[k] = c;
+                const int dy = 2 * (cj_lo + r) - a.two_mid;
+                dy2[k] = (uint32_t)(dy * dy);
+            }
             if (!mbar_wait(&full[g % S], (uint32_t)((g / S) & 1), a.status, 3) ||
                 !mbar_wait(&full[(g + 1) % S], (uint32_t)(((g + 1) / S) & 1), a.status, 3))
                 abort_flag = 1;
-            const int rows_out = cj_hi - cj_lo;
-            const int n_it = rows_out * a.c4;
             for (int q = 0; q < ci_hi - ci_lo && !abort_flag; ++q) {
                 const long long gm = g + q, gc = gm + 1, gp = gm + 2;
                 if (!mbar_wait(&full[gp % S], (uint32_t)((gp / S) & 1), a.status, 3)) {
@@ -199,93 +239,162 @@ __global__ void __launch_bounds__(kStreamMaxThreads, 1) stream_step_kernel(Strea
                 const float *Sc = stage0 + (size_t)(gc % S) * stage_floats;
                 const float *Sp = stage0 + (size_t)(gp % S) * stage_floats;
                 const int ci = ci_lo + q;
-                for (int it = ctid; it < n_it; it += nct) {
-                    const int r = it / a.c4;
-                    const int c = it - r * a.c4;
-                    const int cj = cj_lo + r;
+                const int dx = 2 * ci - a.two_mid;
+                const uint32_t dx2 = (uint32_t)(dx * dx);
+                const int64_t pbase = (int64_t)ci * plane_stride;
+                const bool edge_i = (ci == 1) || (ci == n - 2);
+                float rec_acc = 0.f, p_acc = 0.f, n_acc = 0.f;
+#pragma unroll
+                for (int k = 0; k < IPT; ++k) {
+                    const int kd = kind[k], rs = rs_[k], c = c_[k];
                     const int k0 = 4 * c;
-                    const int rs = r + 1;
-                    bool gk[4];
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) gk[e] = (k0 + e >= a.nze) && (k0 + e < a.gap_end);
-                    const bool g_km = (k0 - 1 >= a.nze) && (k0 - 1 < a.gap_end);
-                    const bool g_kp = (k0 + 4 >= a.nze) && (k0 + 4 < a.gap_end);
-                    const int oc = rs * kp + k0;  // offset of the centre vector in a species block
-                    float4 P = lds4(Sc + oc), N = lds4(Sc + spec + oc);
-                    float4 Pjm = lds4(Sc + oc - kp), Njm = lds4(Sc + spec + oc - kp);
-                    float4 Pjp = lds4(Sc + oc + kp), Njp = lds4(Sc + spec + oc + kp);
-                    float4 Pim = lds4(Sm + oc), Nim = lds4(Sm + spec + oc);
-                    float4 Pip = lds4(Sp + oc), Nip = lds4(Sp + spec + oc);
-                    float pkm = c > 0 ? Sc[oc - 1] : 0.f, nkm = c > 0 ? Sc[spec + oc - 1] : 0.f;
-                    float pkp = k0 + 4 < kp ? Sc[oc + 4] : 0.f, nkp = k0 + 4 < kp ? Sc[spec + oc + 4] : 0.f;
-                    const int64_t ccol = (int64_t)ci * n + cj;
+                    const int o = rs * kp + k0;
+                    // convergent part: centre vectors, densities, edge shuffles
+                    float4 P = lds4(Sc + o), N = lds4(Sc + spec + o);
                     const float dens_c = Sc[dens_off + rs];
-                    if (a.dens) {
-                        const float dc = a.gfac * dens_c;
-                        const float dim = a.gfac * Sm[dens_off + rs], dip = a.gfac * Sp[dens_off + rs];
-                        const float djm = a.gfac * Sc[dens_off + rs - 1], djp = a.gfac * Sc[dens_off + rs + 1];
-                        add_dep(P, dc, gk);
-                        add_dep(N, dc, gk);
-                        add_dep(Pjm, djm, gk);
-                        add_dep(Njm, djm, gk);
-                        add_dep(Pjp, djp, gk);
-                        add_dep(Njp, djp, gk);
-                        add_dep(Pim, dim, gk);
-                        add_dep(Nim, dim, gk);
-                        add_dep(Pip, dip, gk);
-                        add_dep(Nip, dip, gk);
-                        if (g_km) { pkm += dc; nkm += dc; }
-                        if (g_kp) { pkp += dc; nkp += dc; }
+                    const float dcen = a.gfac * dens_c;
+                    const float dlat = a.gfac * ((Sc[dens_off + rs - 1] + Sc[dens_off + rs + 1]) +
+                                                 (Sm[dens_off + rs] + Sp[dens_off + rs]));
+                    if (kd == 1) {
+                        P.x += dcen; P.y += dcen; P.z += dcen; P.w += dcen;
+                        N.x += dcen; N.y += dcen; N.z += dcen; N.w += dcen;
                     }
-                    const float pv[6] = {pkm, P.x, P.y, P.z, P.w, pkp};
-                    const float nv[6] = {nkm, N.x, N.y, N.z, N.w, nkp};
-                    const float pl4[4] = {(Pjm.x + Pjp.x) + (Pim.x + Pip.x), (Pjm.y + Pjp.y) + (Pim.y + Pip.y),
-                                          (Pjm.z + Pjp.z) + (Pim.z + Pip.z), (Pjm.w + Pjp.w) + (Pim.w + Pip.w)};
-                    const float nl4[4] = {(Njm.x + Njp.x) + (Nim.x + Nip.x), (Njm.y + Njp.y) + (Nim.y + Nip.y),
-                                          (Njm.z + Njp.z) + (Nim.z + Nip.z), (Njm.w + Njp.w) + (Nim.w + Nip.w)};
-                    const bool scored = scored_column(a.score, ci, cj);
-                    float po[4], no[4];
-                    float rec_sum = 0.f, p_sum = 0.f, n_sum = 0.f;
+                    const float up_p = __shfl_up_sync(0xffffffffu, P.w, 1);
+                    const float up_n = __shfl_up_sync(0xffffffffu, N.w, 1);
+                    const float dn_p = __shfl_down_sync(0xffffffffu, P.x, 1);
+                    const float dn_n = __shfl_down_sync(0xffffffffu, N.x, 1);
+                    if (kd == 0) continue;
+                    const int cj = cj_lo + rs - 1;
+                    const bool scored = (dx2 + dy2[k] <= a.thr4);
+                    float4 PO, NO;
+                    if (kd == 1) {
+                        // ---- core vector: mask-free, packed FP32x2 ----
+                        float pkm, nkm, pkp, nkp;
+                        if (lane > 0 && c > c_lo) {
+                            pkm = up_p;
+                            nkm = up_n;
+                        } else {
+                            const float d = (c > c_lo || gap_below) ? dcen : 0.f;
+                            pkm = Sc[o - 1] + d;
+                            nkm = Sc[spec + o - 1] + d;
+                        }
+                        if (lane < 31 && c < c_hi - 1) {
+                            pkp = dn_p;
+                            nkp = dn_n;
+                        } else {
+                            const float d = (c < c_hi - 1 || gap_above) ? dcen : 0.f;
+                            pkp = Sc[o + 4] + d;
+                            nkp = Sc[spec + o + 4] + d;
+                        }
+                        const float4 Pjm = lds4(Sc + o - kp), Pjp = lds4(Sc + o + kp);
+                        const float4 Pim = lds4(Sm + o), Pip = lds4(Sp + o);
+                        const float2 DL = make_float2(dlat, dlat);
+                        const float2 Llo = __fadd2_rn(__fadd2_rn(__fadd2_rn(make_float2(Pjm.x, Pjm.y), make_float2(Pjp.x, Pjp.y)),
+                                                                 __fadd2_rn(make_float2(Pim.x, Pim.y), make_float2(Pip.x, Pip.y))), DL);
+                        const float2 Lhi = __fadd2_rn(__fadd2_rn(__fadd2_rn(make_float2(Pjm.z, Pjm.w), make_float2(Pjp.z, Pjp.w)),
+                                                                 __fadd2_rn(make_float2(Pim.z, Pim.w), make_float2(Pip.z, Pip.w))), DL);
+                        const float4 Njm = lds4(Sc + spec + o - kp), Njp = lds4(Sc + spec + o + kp);
+                        const float4 Nim = lds4(Sm + spec + o), Nip = lds4(Sp + spec + o);
+                        const float2 Mlo = __fadd2_rn(__fadd2_rn(__fadd2_rn(make_float2(Njm.x, Njm.y), make_float2(Njp.x, Njp.y)),
+                                                                 __fadd2_rn(make_float2(Nim.x, Nim.y), make_float2(Nip.x, Nip.y))), DL);
+                        const float2 Mhi = __fadd2_rn(__fadd2_rn(__fadd2_rn(make_float2(Njm.z, Njm.w), make_float2(Njp.z, Njp.w)),
+                                                                 __fadd2_rn(make_float2(Nim.z, Nim.w), make_float2(Nip.z, Nip.w))), DL);
+                        const float2 Plo = make_float2(P.x, P.y), Phi = make_float2(P.z, P.w);
+                        const float2 Nlo = make_float2(N.x, N.y), Nhi = make_float2(N.z, N.w);
+                        // positive: zm * n[k-1] + zp * n[k+1] + lat * L + cen * n
+                        float2 plo = __ffma2_rn(CENp, Plo, __ffma2_rn(LATp, Llo, __ffma2_rn(ZPp, make_float2(P.y, P.z), __fmul2_rn(ZMp, make_float2(pkm, P.x)))));
+                        float2 phi = __ffma2_rn(CENp, Phi, __ffma2_rn(LATp, Lhi, __ffma2_rn(ZPp, make_float2(P.w, pkp), __fmul2_rn(ZMp, make_float2(P.y, P.z)))));
+                        // negative drifts the other way: zm on k+1, zp on k-1
+                        float2 nlo = __ffma2_rn(CENn, Nlo, __ffma2_rn(LATn, Mlo, __ffma2_rn(ZPn, make_float2(nkm, N.x), __fmul2_rn(ZMn, make_float2(N.y, N.z)))));
+                        float2 nhi = __ffma2_rn(CENn, Nhi, __ffma2_rn(LATn, Mhi, __ffma2_rn(ZPn, make_float2(N.y, N.z), __fmul2_rn(ZMn, make_float2(N.w, nkp)))));
+                        const float2 rlo = __fmul2_rn(__fmul2_rn(ADT, Plo), Nlo);
+                        const float2 rhi = __fmul2_rn(__fmul2_rn(ADT, Phi), Nhi);
+                        plo = __ffma2_rn(rlo, NEG1, plo);
+                        phi = __ffma2_rn(rhi, NEG1, phi);
+                        nlo = __ffma2_rn(rlo, NEG1, nlo);
+                        nhi = __ffma2_rn(rhi, NEG1, nhi);
+                        PO = make_float4(plo.x, plo.y, phi.x, phi.y);
+                        NO = make_float4(nlo.x, nlo.y, nhi.x, nhi.y);
+                        if (scored) {
+                            const float2 rs2 = __fadd2_rn(rlo, rhi), ps2 = __fadd2_rn(plo, phi), ns2 = __fadd2_rn(nlo, nhi);
+                            rec_acc += rs2.x + rs2.y;
+                            p_acc += ps2.x + ps2.y;
+                            n_acc += ns2.x + ns2.y;
+                        }
+                    } else {
+                        // ---- edge vector: per-element gap and validity masks ----
+                        float gk[4];
+                        bool valid[4];
 #pragma unroll
-                    for (int e = 0; e < 4; ++e) {
-                        const int k = k0 + e;
-                        const float p = pv[e + 1], nn = nv[e + 1];
-                        const float p_new = a.p_zm * pv[e] + a.p_zp * pv[e + 2] + a.p_lat * pl4[e] + a.p_cen * p;
-                        const float n_new = a.n_zm * nv[e + 2] + a.n_zp * nv[e] + a.n_lat * nl4[e] + a.n_cen * nn;
-                        const float rec = a.alpha_dt * p * nn;
-                        const bool valid = (k >= 1) && (k <= a.nzb - 2);
-                        po[e] = valid ? p_new - rec : 0.f;
-                        no[e] = valid ? n_new - rec : 0.f;
-                        if (scored && gk[e]) {
-                            rec_sum += rec;
-                            p_sum += po[e];
-                            n_sum += no[e];
+                        for (int e = 0; e < 4; ++e) {
+                            const int kk = k0 + e;
+                            gk[e] = (kk >= a.nze && kk < a.gap_end) ? 1.f : 0.f;
+                            valid[e] = kk >= 1 && kk <= a.nzb - 2;
+                        }
+                        P.x = fmaf(gk[0], dcen, P.x); P.y = fmaf(gk[1], dcen, P.y);
+                        P.z = fmaf(gk[2], dcen, P.z); P.w = fmaf(gk[3], dcen, P.w);
+                        N.x = fmaf(gk[0], dcen, N.x); N.y = fmaf(gk[1], dcen, N.y);
+                        N.z = fmaf(gk[2], dcen, N.z); N.w = fmaf(gk[3], dcen, N.w);
+                        const bool g_km = (k0 - 1 >= a.nze && k0 - 1 < a.gap_end);
+                        const bool g_kp = (k0 + 4 >= a.nze && k0 + 4 < a.gap_end);
+                        const float pkm = c > 0 ? Sc[o - 1] + (g_km ? dcen : 0.f) : 0.f;
+                        const float nkm = c > 0 ? Sc[spec + o - 1] + (g_km ? dcen : 0.f) : 0.f;
+                        const float pkp = c + 1 < c4 ? Sc[o + 4] + (g_kp ? dcen : 0.f) : 0.f;
+                        const float nkp = c + 1 < c4 ? Sc[spec + o + 4] + (g_kp ? dcen : 0.f) : 0.f;
+                        const float4 Pjm = lds4(Sc + o - kp), Pjp = lds4(Sc + o + kp);
+                        const float4 Njm = lds4(Sc + spec + o - kp), Njp = lds4(Sc + spec + o + kp);
+                        const float4 Pim = lds4(Sm + o), Pip = lds4(Sp + o);
+                        const float4 Nim = lds4(Sm + spec + o), Nip = lds4(Sp + spec + o);
+                        const float pv[6] = {pkm, P.x, P.y, P.z, P.w, pkp};
+                        const float nv[6] = {nkm, N.x, N.y, N.z, N.w, nkp};
+                        const float pl4[4] = {fmaf(gk[0], dlat, (Pjm.x + Pjp.x) + (Pim.x + Pip.x)),
+                                              fmaf(gk[1], dlat, (Pjm.y + Pjp.y) + (Pim.y + Pip.y)),
+                                              fmaf(gk[2], dlat, (Pjm.z + Pjp.z) + (Pim.z + Pip.z)),
+                                              fmaf(gk[3], dlat, (Pjm.w + Pjp.w) + (Pim.w + Pip.w))};
+                        const float nl4[4] = {fmaf(gk[0], dlat, (Njm.x + Njp.x) + (Nim.x + Nip.x)),
+                                              fmaf(gk[1], dlat, (Njm.y + Njp.y) + (Nim.y + Nip.y)),
+                                              fmaf(gk[2], dlat, (Njm.z + Njp.z) + (Nim.z + Nip.z)),
+                                              fmaf(gk[3], dlat, (Njm.w + Njp.w) + (Nim.w + Nip.w))};
+                        float po[4], no[4];
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            const float p = pv[e + 1], nn = nv[e + 1];
+                            const float p_new = a.p_zm * pv[e] + a.p_zp * pv[e + 2] + a.p_lat * pl4[e] + a.p_cen * p;
+                            const float n_new = a.n_zm * nv[e + 2] + a.n_zp * nv[e] + a.n_lat * nl4[e] + a.n_cen * nn;
+                            const float rec = a.alpha_dt * p * nn;
+                            po[e] = valid[e] ? p_new - rec : 0.f;
+                            no[e] = valid[e] ? n_new - rec : 0.f;
+                            if (scored && gk[e] != 0.f) {
+                                rec_acc += rec;
+                                p_acc += po[e];
+                                n_acc += no[e];
+                            }
+                        }
+                        PO = make_float4(po[0], po[1], po[2], po[3]);
+                        NO = make_float4(no[0], no[1], no[2], no[3]);
+                        const int64_t ccol = (int64_t)ci * n + cj;
+                        if (c == 0) {
+                            if (scored && a.dens) t_inj.add(dens_c);
+                            if (a.dens_zero) a.dens_zero[ccol] = 0.f;
                         }
                     }
-                    const float4 PO = make_float4(po[0], po[1], po[2], po[3]);
-                    const float4 NO = make_float4(no[0], no[1], no[2], no[3]);
-                    st4(a.pos_out + ccol * kp + k0, PO);
-                    st4(a.neg_out + ccol * kp + k0, NO);
-                    if (scored) {
-                        t_rec.add(rec_sum);
-                        t_p.add(p_sum);
-                        t_n.add(n_sum);
-                        if (c == 0 && a.dens) t_inj.add(dens_c);
-                    }
-                    if (c == 0 && a.dens_zero) a.dens_zero[ccol] = 0.f;
+                    const int64_t out = pbase + (int64_t)cj * kp + k0;
+                    st4(a.pos_out + out, PO);
+                    st4(a.neg_out + out, NO);
 
                     // ring columns attached to this interior column
-                    const bool lo_i = (ci == 1), hi_i = (ci == n - 2), lo_j = (cj == 1), hi_j = (cj == n - 2);
-                    if (lo_i || hi_i || lo_j || hi_j) {
+                    const bool lo_j = (cj == 1), hi_j = (cj == n - 2);
+                    if (edge_i || lo_j || hi_j) {
+                        const bool lo_i = (ci == 1), hi_i = (ci == n - 2);
                         // up to three targets: (ri, cj), (ci, rj), (ri, rj)
                         for (int tgt = 0; tgt < 3; ++tgt) {
                             int ri = ci, rj = cj;
-                            const float *S = Sc;
+                            const float *Sr = Sc;
                             int row = rs;
                             if (tgt == 0) {
                                 if (!(lo_i || hi_i)) continue;
                                 ri = lo_i ? 0 : n - 1;
-                                S = lo_i ? Sm : Sp;
+                                Sr = lo_i ? Sm : Sp;
                             } else if (tgt == 1) {
                                 if (!(lo_j || hi_j)) continue;
                                 rj = lo_j ? 0 : n - 1;
@@ -294,7 +403,7 @@ __global__ void __launch_bounds__(kStreamMaxThreads, 1) stream_step_kernel(Strea
                                 if (!((lo_i || hi_i) && (lo_j || hi_j))) continue;
                                 ri = lo_i ? 0 : n - 1;
                                 rj = lo_j ? 0 : n - 1;
-                                S = lo_i ? Sm : Sp;
+                                Sr = lo_i ? Sm : Sp;
                                 row = lo_j ? rs - 1 : rs + 1;
                             }
                             const int64_t rcol = (int64_t)ri * n + rj;
@@ -302,11 +411,14 @@ __global__ void __launch_bounds__(kStreamMaxThreads, 1) stream_step_kernel(Strea
                                 st4(a.pos_out + rcol * kp + k0, PO);
                                 st4(a.neg_out + rcol * kp + k0, NO);
                             } else {
-                                float4 RP = lds4(S + row * kp + k0), RN = lds4(S + spec + row * kp + k0);
-                                if (a.dens) {
-                                    const float d = a.gfac * S[dens_off + row];
-                                    add_dep(RP, d, gk);
-                                    add_dep(RN, d, gk);
+                                float4 RP = lds4(Sr + row * kp + k0), RN = lds4(Sr + spec + row * kp + k0);
+                                const float d = a.gfac * Sr[dens_off + row];
+#pragma unroll
+                                for (int e = 0; e < 4; ++e) {
+                                    const int kk = k0 + e;
+                                    const float de = (kk >= a.nze && kk < a.gap_end) ? d : 0.f;
+                                    (&RP.x)[e] += de;
+                                    (&RN.x)[e] += de;
                                 }
                                 st4(a.pos_out + rcol * kp + k0, RP);
                                 st4(a.neg_out + rcol * kp + k0, RN);
@@ -315,6 +427,9 @@ __global__ void __launch_bounds__(kStreamMaxThreads, 1) stream_step_kernel(Strea
                         }
                     }
                 }
+                t_rec.add(rec_acc);
+                t_p.add(p_acc);
+                t_n.add(n_acc);
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&empty[gm % S]);
             }
@@ -329,6 +444,19 @@ __global__ void __launch_bounds__(kStreamMaxThreads, 1) stream_step_kernel(Strea
     }
     double v[4] = {t_inj.value(), t_rec.value(), t_p.value(), t_n.value()};
     finish_tally_rt(v, a.partials, a.counter, a.tally, a.injected_scale);
+}
+
+template <int IPT>
+static int launch_ipt(const StreamArgs &a, unsigned blocks, int threads, int smem, cudaStream_t st) {
+    static int configured = 0;  // per instantiation: largest dynamic smem set so far
+    if (smem > configured) {
+        cudaError_t e =
+            cudaFuncSetAttribute(stream_step_kernel<IPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return set_cuda_error("cudaFuncSetAttribute(stream_step_kernel)", e);
+        configured = smem;
+    }
+    stream_step_kernel<IPT><<<blocks, threads, smem, st>>>(a);
+    return check_launch("stream_step_kernel");
 }
 
 int stream_smem_bytes(int tj, int kp, int stages) {
@@ -368,21 +496,30 @@ int launch_stream_step(const pic_grid *g, const StreamShape &sh, const void *pos
     a.n_lat = (float)g->n_lat; a.n_zm = (float)g->n_zm; a.n_zp = (float)g->n_zp; a.n_cen = (float)g->n_cen;
     a.alpha_dt = (float)g->alpha_dt;
     a.gfac = (float)g->gaussian_factor;
-    int rc = score_test(g, &a.score);
+    ScoreTest sc;
+    int rc = score_test(g, &sc);
     if (rc) return rc;
+    if (g->no_xy > 16383) return set_error(PIC_E_CAPACITY, "stream variant: no_xy must be <= 16383");
+    a.two_mid = (int)sc.two_mid;
+    // (2i - two_mid)^2 + (2j - two_mid)^2 < 2^31 for no_xy <= 16383
+    a.thr4 = sc.thr4 < 0 ? 0u : (sc.thr4 > 0x7fffffffLL ? 0xffffffffu : (uint32_t)sc.thr4);
     a.injected_scale = g->gaussian_factor * (double)g->no_z;
     const int smem = stream_smem_bytes(a.tj, a.kp, a.stages);
-    static int configured = 0;
-    if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(stream_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return set_cuda_error("cudaFuncSetAttribute(stream_step_kernel)", e);
-        configured = smem;
-    }
     int64_t blocks = (int64_t)sh.sm_count * sh.ctas_per_sm;
     if (blocks > a.n_items) blocks = a.n_items;
     if (blocks > kMaxStepBlocks) blocks = kMaxStepBlocks;
-    stream_step_kernel<<<(unsigned)blocks, (a.consumer_warps + 1) * 32, smem, st>>>(a);
-    return check_launch("stream_step_kernel");
+    const int threads = (a.consumer_warps + 1) * 32;
+    const int ipt = (a.tj * a.c4 + a.consumer_warps * 32 - 1) / (a.consumer_warps * 32);
+    if (ipt >= 1 && ipt <= 4 && threads > stream_max_threads(ipt))
+        return set_error(PIC_E_INVALID, "stream variant: too many consumer warps for this tile (registers)");
+    switch (ipt) {
+        case 1: return launch_ipt<1>(a, (unsigned)blocks, threads, smem, st);
+        case 2: return launch_ipt<2>(a, (unsigned)blocks, threads, smem, st);
+        case 3: return launch_ipt<3>(a, (unsigned)blocks, threads, smem, st);
+        case 4: return launch_ipt<4>(a, (unsigned)blocks, threads, smem, st);
+        default:
+            return set_error(PIC_E_INVALID, "stream variant: tile_rows x k-vectors exceed 4 items per consumer thread");
+    }
 }
 
 }  // namespace pic

@@ -80,6 +80,12 @@ def test_invalid_grid_is_refused_before_any_device_work(lib):
     g.kpitch, g.nze = 16, 0
     assert lib.pic_step_workspace_bytes(ctypes.byref(g), ctypes.byref(b)) == native.PIC_E_INVALID
     g.nze = 3
+    g.mid_xy, g.scoring_radius_sq = 4.3, 9.0
+    assert lib.pic_step_workspace_bytes(ctypes.byref(g), ctypes.byref(b)) == native.PIC_E_INVALID
+    assert b"mid_xy" in lib.pic_last_error()
+    g.mid_xy, g.scoring_radius_sq = 4.0, 0.0
+    assert lib.pic_step_workspace_bytes(ctypes.byref(g), ctypes.byref(b)) == native.PIC_E_INVALID
+    g.scoring_radius_sq = 9.0
     assert lib.pic_step_workspace_bytes(ctypes.byref(g), ctypes.byref(b)) == native.PIC_OK
     assert b.value > 0
     rc = lib.pic_step(ctypes.byref(g), None, None, None, None, None, None, None, None, 0, None)
@@ -111,7 +117,7 @@ def test_launch_shape_resolution_without_a_gpu():
     big = eng.make_grid(make_config("full_electrode_5um_10p"))
     s = eng.resolve_shape(big)
     assert s["variant"] == "stream"
-    assert s["tile_rows"] == 10 and s["stages"] == 5 and s["consumer_warps"] == 16
+    assert s["tile_rows"] == 7 and s["consumer_warps"] == 12 and s["stages"] >= 4
     small = eng.make_grid(make_config("column_10um_r008"))
     assert eng.resolve_shape(small)["variant"] == "flat"
     f64 = eng.make_grid(make_config("full_electrode_5um_10p"), dtype="float64")
