@@ -145,6 +145,28 @@ int pic_step(const pic_grid *g, const void *pos_in, const void *neg_in, void *po
              uintptr_t stream);
 
 /*
+ * pic_step_noalloc -- one whole time step, allocating nothing: this step's
+ * n_tracks track centres deposited (as pic_deposit, counts updated), then the
+ * fused step (as pic_step) from pos_in/neg_in into pos_out/neg_out, tallies
+ * into tally[0..3]. The 2D density and the tally workspace live in a static
+ * device array inside the library, so a caller that cannot allocate device
+ * memory -- a binding that only holds buffers owned by another runtime, or
+ * code running where cudaMalloc is not allowed -- passes only its inputs and
+ * outputs.
+ *
+ * No counterpart in the reference (whose drivers allocate their own arrays).
+ * Limit: the 2D density must fit the 8 MiB static scratch -- no_xy^2 <= 2^21
+ * for float32 fields, <= 2^20 for float64 -- else PIC_E_CAPACITY. Every GPU
+ * that loads the library holds the array (8 MiB plus the tally workspace)
+ * until exit. All calls share it: calls that overlap on the GPU race, so
+ * serialise them. The first call on a device looks up the array's device
+ * address; make it before any stream capture.
+ */
+int pic_step_noalloc(const pic_grid *g, const void *pos_in, const void *neg_in, void *pos_out, void *neg_out,
+                     const double *xs, const double *ys, int64_t n_tracks, uint32_t *counts, double *tally,
+                     uintptr_t stream);
+
+/*
  * pic_run_segment -- n_steps consecutive time steps on the device.
  *
  * Step s (0-based within the segment) reads fields[(parity + s) & 1] and

@@ -88,6 +88,11 @@ EXPORTS = {
         [ctypes.POINTER(PicGrid), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p],
     ),
+    "pic_step_noalloc": (
+        ctypes.c_int,
+        [ctypes.POINTER(PicGrid), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
+    ),
     "pic_run_segment": (
         ctypes.c_int,
         [ctypes.POINTER(PicGrid), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

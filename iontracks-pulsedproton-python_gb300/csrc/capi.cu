@@ -273,6 +273,20 @@ int pic_step(const pic_grid *g, const void *pos_in, const void *neg_in, void *po
                        reinterpret_cast<cudaStream_t>(stream));
 }
 
+int pic_step_noalloc(const pic_grid *g, const void *pos_in, const void *neg_in, void *pos_out, void *neg_out,
+                     const double *xs, const double *ys, int64_t n_tracks, uint32_t *counts, double *tally,
+                     uintptr_t stream) {
+    int rc = check_grid(g);
+    if (rc) return rc;
+    if ((rc = check_fields(pos_in, neg_in, pos_out, neg_out))) return rc;
+    if (pos_in == pos_out || neg_in == neg_out) return set_error(PIC_E_INVALID, "input and output fields must differ");
+    if (!tally || !counts) return set_error(PIC_E_INVALID, "null pointer argument");
+    if (n_tracks < 0) return set_error(PIC_E_INVALID, "n_tracks must be >= 0");
+    if (n_tracks > 0 && (!xs || !ys)) return set_error(PIC_E_INVALID, "track arrays are null");
+    return step_noalloc(g, pos_in, neg_in, pos_out, neg_out, xs, ys, n_tracks, counts, tally,
+                        reinterpret_cast<cudaStream_t>(stream));
+}
+
 int pic_run_segment(const pic_grid *g, void *pos0, void *neg0, void *pos1, void *neg1, int64_t parity,
                     int64_t n_steps, const double *xs, const double *ys, const int64_t *track_offsets,
                     void *dens0, void *dens1, int64_t dens_parity, uint32_t *counts, double *tally,
