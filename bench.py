@@ -158,17 +158,18 @@ def _interior(cfg):
     return (cfg.no_xy - 2) ** 2 * (cfg.no_z_with_buffer - 2)
 
 
-def cpu_sample(cfg, steps=2, threads=None):
-    """FP64 oracle (the reference algorithm in C/OpenMP) on the first
-    ``steps`` pulse steps of the workload; returns (voxel-steps/s, cores)."""
+def cpu_sample(cfg, steps=3, warmup=2, threads=None):
+    """FP64 oracle (the reference algorithm in C/OpenMP, batched deposition)
+    on pulse steps of the workload, on all host cores. The first ``warmup``
+    steps (page first-touch of the 15 GB of float64 fields) are run but not
+    timed; returns (voxel-steps/s, cores, timed seconds)."""
     from oracle import oracle
 
     cores = threads or oracle.cores_used()
     oracle.set_threads(cores)
-    t0 = time.perf_counter()
-    res = oracle.run(cfg, mode="batched", max_steps=steps, keep_fields=False)
-    _ = time.perf_counter() - t0
-    return _interior(cfg) * res["steps"] / res["wall_s"], cores, res["wall_s"]
+    res = oracle.run(cfg, mode="batched", max_steps=warmup + steps, keep_fields=False)
+    timed = float(res["step_wall_s"][warmup:].sum())
+    return _interior(cfg) * steps / timed, cores, timed
 
 
 def run_reference(args):
@@ -177,17 +178,15 @@ def run_reference(args):
         return 0
     desc, cfg = _config(args.workload)
     steps = max(1, args.ref_steps)
-    vals = []
-    cores = None
-    v, cores, wall = cpu_sample(cfg, steps=steps)
-    vals.append(v)
+    v, cores, wall = cpu_sample(cfg, steps=steps, warmup=min(args.warmup, 2))
     line = {
         "impl": "reference", "metric": "interior voxel-steps/s", "value": v, "unit": "voxel-steps/s",
-        "n_gpus": world, "steps": steps, "warmup": 0, "ms_per_step": wall / steps * 1e3,
+        "n_gpus": world, "steps": steps, "warmup": min(args.warmup, 2), "ms_per_step": wall / steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": desc},
         "cpu_baseline": {"value": v, "unit": "voxel-steps/s", "cores": cores, "kind": "port",
-                         "sample": f"first {steps} pulse steps of the workload (deposition + sweep), FP64 oracle"},
+                         "sample": f"{steps} pulse steps of the workload (deposition + sweep) after 2 untimed, "
+                                   "FP64 oracle (C/OpenMP restatement of the reference kernels)"},
         "e2e": {"value": v, "unit": "voxel-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -216,6 +215,11 @@ def run_gb300(args):
     xs, ys = pkg.TrackSampler(rng, cfg.mid_xy, cfg.sampling_radius, cfg.no_xy).sample(int(counts.sum()))
     shape = _shape(args)
     eng = eng_mod.ChamberEngine(cfg, dtype=args.dtype, max_tracks=len(xs), tally_steps=n_steps, shape=shape)
+    tuned = None
+    if args.variant == "auto" and not args.no_tune:
+        at = importlib.import_module(PACKAGE + ".autotune")
+        tuned = at.tune(eng, quick=True, reps=5)
+        shape = dict(tuned["shape"])
     resolved = eng_mod.resolve_shape(eng.grid)
     eng.upload_tracks(xs, ys, non_blocking=False)
     off = np.zeros(n_steps + 1, dtype=np.int64)
@@ -265,8 +269,11 @@ def run_gb300(args):
         cur ^= 1
     torch.cuda.synchronize()
     step_ms = statistics.median(a.elapsed_time(b) for a, b in evs)
+    at = importlib.import_module(PACKAGE + ".autotune")
+    idle_ms = at.time_shape(eng, resolved, reps=reps, with_deposition=False)
     peak, peak_kind = _peaks()
     achieved = BYTES_PER_VOXEL_STEP * vox / (step_ms / 1e3) / 1e9
+    idle_achieved = BYTES_PER_VOXEL_STEP * vox / (idle_ms / 1e3) / 1e9
     traffic = _traffic_bytes(args.workload)
     eng.close()
     del eng
@@ -292,7 +299,8 @@ def run_gb300(args):
     if rank == 0 and not args.no_cpu:
         v, cores, wall = cpu_sample(cfg, steps=args.ref_steps)
         cpu = {"value": v, "unit": "voxel-steps/s", "cores": cores, "kind": "port",
-               "sample": f"first {args.ref_steps} pulse steps of the same workload, FP64 oracle, {wall:.1f} s"}
+               "sample": f"{args.ref_steps} pulse steps of the same workload after 2 untimed (page first-touch), "
+                         f"FP64 oracle, {wall:.1f} s timed"}
 
     if rank == 0:
         line = {
@@ -309,7 +317,10 @@ def run_gb300(args):
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                          "kernel": "stream_step_kernel" if resolved["variant"] == "stream" else "step_kernel",
                          "kernel_ms": step_ms,
-                         "algorithmic_bytes_per_launch": BYTES_PER_VOXEL_STEP * vox},
+                         "algorithmic_bytes_per_launch": BYTES_PER_VOXEL_STEP * vox,
+                         "idle_step": {"kernel_ms": idle_ms, "achieved": idle_achieved, "frac": idle_achieved / peak,
+                                       "note": "the same kernel on a step without deposition (97 % of the "
+                                               "steps of the 10-pulse run)"}},
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": launches,
@@ -330,8 +341,9 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="full_electrode_5um")
     ap.add_argument("--dtype", choices=["float32", "float64"], default="float32")
     ap.add_argument("--e2e-steps", type=int, default=600)
-    ap.add_argument("--ref-steps", type=int, default=2)
+    ap.add_argument("--ref-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner")
     ap.add_argument("--variant", choices=["auto", "flat", "stream"], default="auto")
     ap.add_argument("--tile-rows", dest="tile_rows", type=int, default=0)
     ap.add_argument("--planes-per-item", dest="planes_per_item", type=int, default=0)

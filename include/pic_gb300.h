@@ -14,7 +14,9 @@
  * k fastest, kpitch = pic_kpitch(nzb) >= nzb (rows start 32-byte aligned).
  * Elements k >= nzb - 1 and k == 0 are the z end planes plus padding and are
  * kept at zero. Fields are float32 (PIC_F32) or float64 (PIC_F64, the
- * validation build); the 2D density follows the field type. Per-step tallies
+ * validation build); the 2D density follows the field type and is laid out
+ * dens[i][j], 0 <= j < pic_dens_pitch(no_xy) (rows padded to 4 elements so
+ * each starts 16-byte aligned). Per-step tallies
  * are always float64: tally[s] = {injected, recombined, sum n+, sum n-} over
  * the scored voxels.
  */
@@ -83,6 +85,9 @@ int pic_abi_version(void);
 
 /* k pitch for a given no_z_with_buffer: nzb rounded up to 8 elements. */
 int64_t pic_kpitch(int64_t nzb);
+
+/* Row pitch of the 2D density: no_xy rounded up to 4 elements. */
+int64_t pic_dens_pitch(int64_t no_xy);
 
 /* Checks that a CUDA device of compute capability 10.3 is current; fills the
  * SM count and the device's total memory. */
@@ -155,8 +160,8 @@ int pic_step(const pic_grid *g, const void *pos_in, const void *neg_in, void *po
  * outputs.
  *
  * No counterpart in the reference (whose drivers allocate their own arrays).
- * Limit: the 2D density must fit the 8 MiB static scratch -- no_xy^2 <= 2^21
- * for float32 fields, <= 2^20 for float64 -- else PIC_E_CAPACITY. Every GPU
+ * Limit: the 2D density must fit the 8 MiB static scratch -- no_xy <= 1448
+ * for float32 fields, <= 1024 for float64 -- else PIC_E_CAPACITY. Every GPU
  * that loads the library holds the array (8 MiB plus the tally workspace)
  * until exit. All calls share it: calls that overlap on the GPU race, so
  * serialise them. The first call on a device looks up the array's device

@@ -68,6 +68,7 @@ EXPORTS = {
     "pic_last_error": (ctypes.c_char_p, []),
     "pic_abi_version": (ctypes.c_int, []),
     "pic_kpitch": (ctypes.c_int64, [ctypes.c_int64]),
+    "pic_dens_pitch": (ctypes.c_int64, [ctypes.c_int64]),
     "pic_device_info": (
         ctypes.c_int,
         [ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32),

@@ -33,15 +33,16 @@ def candidate_shapes(grid, quick: bool = False) -> list[dict]:
     out = [{"variant": "flat"}]
     if grid.dtype != N.PIC_F32 or grid.no_xy < 16:
         return out
+    out.append({"variant": "stream"})  # the library's own default shape
     kp = grid.kpitch
-    tjs = (3, 5, 8, 10) if quick else (2, 3, 4, 5, 6, 8, 10, 12)
+    tjs = (3, 5, 7, 10) if quick else (2, 3, 4, 5, 6, 7, 8, 10, 12)
     cws = (8, 12, 16) if quick else (4, 6, 8, 10, 12, 16)
     planes = (64,) if quick else (32, 64, 128)
     stage_counts = (4, 6, 8) if quick else (4, 5, 6, 8, 10, 12, 16)
     for tj, cw, ctas, stages, li in itertools.product(tjs, cws, (1, 2), stage_counts, planes):
         if tj > grid.no_xy - 2:
             continue
-        smem = (2 * stages * 8 + 127) // 128 * 128 + stages * (2 * (tj + 2) * kp + ((tj + 5) & ~3)) * 4
+        smem = (2 * stages * 8 + 127) // 128 * 128 + stages * (2 * (tj + 2) * kp + ((tj + 8) & ~3)) * 4
         if ctas * (smem + 3 * 1024) > _SMEM_PER_SM:
             continue
         ipt = -(-(tj * (kp // 4)) // (cw * 32))

@@ -105,7 +105,7 @@ int resolve_shape(pic_grid *g) {
                                                 " consumer warps exceed the register budget of " +
                                                 std::to_string(ipt) + " items per thread");
     }
-    const int stage_bytes = (2 * (g->tile_rows + 2) * kp + ((g->tile_rows + 2 + 3) & ~3)) * 4;
+    const int stage_bytes = (2 * (g->tile_rows + 2) * kp + ((g->tile_rows + 8) & ~3)) * 4;
     // static shared memory of the kernel (reduction scratch, flags) is < 2 KB
     const int budget = kStreamMaxSmem - 2048;
     if (g->stages <= 0) {
@@ -198,6 +198,8 @@ const char *pic_last_error(void) { return g_last_error.c_str(); }
 int pic_abi_version(void) { return 2; }
 
 int64_t pic_kpitch(int64_t nzb) { return (nzb + 7) / 8 * 8; }
+
+int64_t pic_dens_pitch(int64_t no_xy) { return dens_pitch(no_xy); }
 
 int pic_device_info(int32_t *sm_count, int64_t *total_bytes, int32_t *cc_major, int32_t *cc_minor) {
     int dev = 0;

@@ -10,7 +10,8 @@
 // [ceil(x - cut), floor(x + cut)] clipped to [0, no_xy), as in
 // solver_numba.py:86-89.
 //
-// One warp per track. Lanes own stencil columns j; row factors are computed
+// The density is laid out [no_xy][dens_pitch(no_xy)] (rows padded to 16
+// bytes). One warp per track. Lanes own stencil columns j; row factors are computed
 // 32 rows at a time, one row per lane, and broadcast by shuffle. Each cell is
 // added with a float atomic: tracks overlap, and the L2 resolves the
 // collisions. The offset (i - x) is formed in float64 from the float64 track
@@ -35,7 +36,7 @@ template <typename T, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) deposit_kernel(const double *__restrict__ xs,
                                                               const double *__restrict__ ys, int64_t m,
                                                               T *__restrict__ dens, uint32_t *__restrict__ counts,
-                                                              int64_t n, double cut, T h2b2) {
+                                                              int64_t n, int64_t dp, double cut, T h2b2) {
     const int lane = threadIdx.x & 31;
     const int64_t t = (int64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
     if (t >= m) return;
@@ -60,7 +61,7 @@ __global__ void __launch_bounds__(WARPS * 32) deposit_kernel(const double *__res
             const T gi_lane = lane < rows ? gauss1((double)(ib + lane) - x, h2b2) : T(0);
             for (int r = 0; r < rows; ++r) {
                 const T gi = __shfl_sync(0xffffffffu, gi_lane, r);
-                if (jok) atomicAdd(dens + (ib + r) * n + j, gi * gj);
+                if (jok) atomicAdd(dens + (ib + r) * dp + j, gi * gj);
             }
         }
     }
@@ -73,10 +74,11 @@ int launch_deposit(const pic_grid *g, const double *xs, const double *ys, int64_
     const int64_t blocks = (m + WARPS - 1) / WARPS;
     if (g->dtype == PIC_F64) {
         deposit_kernel<double, WARPS><<<(unsigned)blocks, WARPS * 32, 0, st>>>(
-            xs, ys, m, (double *)dens, counts, g->no_xy, g->cutoff_voxels, g->h2_over_b2);
+            xs, ys, m, (double *)dens, counts, g->no_xy, dens_pitch(g->no_xy), g->cutoff_voxels, g->h2_over_b2);
     } else {
         deposit_kernel<float, WARPS><<<(unsigned)blocks, WARPS * 32, 0, st>>>(
-            xs, ys, m, (float *)dens, counts, g->no_xy, g->cutoff_voxels, (float)g->h2_over_b2);
+            xs, ys, m, (float *)dens, counts, g->no_xy, dens_pitch(g->no_xy), g->cutoff_voxels,
+            (float)g->h2_over_b2);
     }
     return check_launch("deposit_kernel");
 }

@@ -13,9 +13,9 @@
 // outputs (next fields, track histogram, tallies).
 //
 // Limits and behaviour:
-//   * the array holds the 2D density of up to kNoAllocDensBytes (8 MiB):
-//     no_xy^2 <= 2^21 for float32 fields (no_xy <= 1448), <= 2^20 for
-//     float64 (no_xy <= 1024); larger grids are refused with PIC_E_CAPACITY;
+//   * the array holds the 2D density (rows padded to 4 elements) of up to
+//     kNoAllocDensBytes (8 MiB): no_xy <= 1448 for float32 fields, <= 1024
+//     for float64; larger grids are refused with PIC_E_CAPACITY;
 //   * every GPU that loads the library holds the array (8 MiB + the tally
 //     workspace) until the process exits;
 //   * every call shares the array and it keeps the last call's contents: the
@@ -66,7 +66,7 @@ int step_noalloc(const pic_grid *g, const void *pos_in, const void *neg_in, void
                  const double *xs, const double *ys, int64_t n_tracks, uint32_t *counts, double *tally,
                  cudaStream_t st) {
     const int64_t es = g->dtype == PIC_F64 ? 8 : 4;
-    const int64_t dens_bytes = g->no_xy * g->no_xy * es;
+    const int64_t dens_bytes = g->no_xy * dens_pitch(g->no_xy) * es;
     if (dens_bytes > kNoAllocDensBytes)
         return set_error(PIC_E_CAPACITY,
                          "pic_step_noalloc: the 2D density of a " + std::to_string(g->no_xy) + " x " +

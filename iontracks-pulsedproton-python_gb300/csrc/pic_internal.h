@@ -68,6 +68,10 @@ __host__ __device__ inline bool scored_column(const ScoreTest &t, int64_t i, int
     return dx * dx + dy * dy <= t.thr4;
 }
 
+// Row pitch of the 2D density: no_xy rounded up to 4 elements, so every row
+// starts 16-byte aligned and a row segment can be fetched by a bulk copy.
+inline int64_t dens_pitch(int64_t no_xy) { return (no_xy + 3) / 4 * 4; }
+
 int set_error(int code, const std::string &msg);
 int set_cuda_error(const char *what, cudaError_t e);
 int check_launch(const char *what);

@@ -37,7 +37,7 @@ struct StepArgs {
     double *tally;
     double *partials;
     unsigned int *counter;
-    int64_t n, kp, c4, items;
+    int64_t n, kp, c4, items, dp;  // dp: density row pitch
     int nzb, nze, gap_end;  // gap = [nze, gap_end)
     int reflecting;
     T p_lat, p_zm, p_zp, p_cen, n_lat, n_zm, n_zp, n_cen, alpha_dt, gfac;
@@ -46,8 +46,8 @@ struct StepArgs {
 };
 
 template <typename T>
-__device__ __forceinline__ T dep_at(const StepArgs<T> &a, int64_t col) {
-    return a.dens ? a.gfac * a.dens[col] : T(0);
+__device__ __forceinline__ T dep_at(const StepArgs<T> &a, int64_t dcol) {
+    return a.dens ? a.gfac * a.dens[dcol] : T(0);
 }
 
 template <typename T, int BLOCK>
@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(BLOCK) step_kernel(StepArgs<T> a) {
         const int c = (int)(item - col * a.c4);
         const int64_t i = col / n, j = col - i * n;
         const int k0 = 4 * c;
-        if (c == 0 && a.dens_zero) a.dens_zero[col] = T(0);
+        if (c == 0 && a.dens_zero) a.dens_zero[i * a.dp + j] = T(0);
 
         // gap mask of the four outputs and of the two z-neighbours
         bool g[4];
@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(BLOCK) step_kernel(StepArgs<T> a) {
         const int64_t out_off = col * kp + k0;
 
         if (ring && !a.reflecting) {
-            const T d = dep_at(a, col);
+            const T d = dep_at(a, i * a.dp + j);
             V4<T> P = load4(a.pos_in + out_off), N = load4(a.neg_in + out_off);
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
@@ -100,10 +100,11 @@ __global__ void __launch_bounds__(BLOCK) step_kernel(StepArgs<T> a) {
         T pkp = k0 + 4 < kp ? a.pos_in[base + 4] : T(0);
         T nkp = k0 + 4 < kp ? a.neg_in[base + 4] : T(0);
 
+        const int64_t dcol = ci * a.dp + cj;
         if (a.dens) {
-            const T dc = a.gfac * a.dens[ccol];
-            const T dim = a.gfac * a.dens[ccol - n], dip = a.gfac * a.dens[ccol + n];
-            const T djm = a.gfac * a.dens[ccol - 1], djp = a.gfac * a.dens[ccol + 1];
+            const T dc = a.gfac * a.dens[dcol];
+            const T dim = a.gfac * a.dens[dcol - a.dp], dip = a.gfac * a.dens[dcol + a.dp];
+            const T djm = a.gfac * a.dens[dcol - 1], djp = a.gfac * a.dens[dcol + 1];
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
                 if (g[e]) {
@@ -151,7 +152,7 @@ __global__ void __launch_bounds__(BLOCK) step_kernel(StepArgs<T> a) {
             t_rec.add(rec_sum);
             t_p.add(p_sum);
             t_n.add(n_sum);
-            if (c == 0 && a.dens) t_inj.add(a.dens[ccol]);
+            if (c == 0 && a.dens) t_inj.add(a.dens[dcol]);
         }
     }
     double v[4] = {t_inj.value(), t_rec.value(), t_p.value(), t_n.value()};
@@ -177,6 +178,7 @@ static int launch_step_t(const pic_grid *g, const void *pos_in, const void *neg_
     a.kp = g->kpitch;
     a.c4 = g->kpitch / 4;
     a.items = g->no_xy * g->no_xy * a.c4;
+    a.dp = dens_pitch(g->no_xy);
     a.nzb = (int)g->nzb;
     a.nze = (int)g->nze;
     a.gap_end = (int)(g->nze + g->no_z);

@@ -39,6 +39,7 @@ struct StreamArgs {
     unsigned int *counter;
     int *status;
     int n, kp, c4, nzb, nze, gap_end, reflecting;
+    int dp;  // density row pitch (multiple of 4 elements)
     int tj, li, jt, n_items, stages, consumer_warps;
     float p_lat, p_zm, p_zp, p_cen, n_lat, n_zm, n_zp, n_cen, alpha_dt, gfac;
     int two_mid;    // 2 * mid_xy
@@ -112,17 +113,18 @@ __global__ void __launch_bounds__(stream_max_threads(IPT), 1) stream_step_kernel
     float *stage0 = reinterpret_cast<float *>(smem_raw + bar_bytes);
     const int rows_max = a.tj + 2;
     const int spec = rows_max * a.kp;       // floats per species in a stage
-    const int dens_off = 2 * spec;          // the plane's density at each staged row
-    const int stage_floats = 2 * spec + ((rows_max + 3) & ~3);
+    const int dens_off = 2 * spec;          // the plane's density row segment
+    const int stage_floats = 2 * spec + ((a.tj + 8) & ~3);
+    const bool has_dens = a.dens != nullptr;
     const int S = a.stages;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int cw = a.consumer_warps;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < S; ++s) {
-            // full: the producer's expect-tx arrival + the arrival after the
-            // density row is staged; the bulk copies' bytes complete it.
-            mbar_init(&full[s], 2);
+            // full: the producer's expect-tx arrival; the bulk copies' bytes
+            // complete it.
+            mbar_init(&full[s], 1);
             mbar_init(&empty[s], cw);
         }
         mbar_fence_init();
@@ -133,41 +135,46 @@ __global__ void __launch_bounds__(stream_max_threads(IPT), 1) stream_step_kernel
     Tally<float> t_rec, t_p, t_n, t_inj;
 
     if (warp == cw) {
-        // ---------------- producer warp ----------------
-        // lane 0 issues the bulk copies; every lane stages one density value
-        // of the plane's rows; lane 0 then arrives a second time.
-        long long g = 0;
-        bool ok = true;
-        for (int w = blockIdx.x; w < a.n_items && ok; w += gridDim.x) {
-            int cj_lo, cj_hi, ci_lo, ci_hi;
-            item_geometry(a, w, cj_lo, cj_hi, ci_lo, ci_hi);
-            const int rows = cj_hi - cj_lo + 2;
-            const uint32_t bytes = (uint32_t)(rows * a.kp * 4);
-            for (int pl = ci_lo - 1; pl <= ci_hi; ++pl, ++g) {
-                const int slot = (int)(g % S);
-                if (g >= S && !mbar_wait(&empty[slot], (uint32_t)(((g / S) - 1) & 1), a.status, 1)) abort_flag = 1;
-                __syncwarp();
-                if (abort_flag) {
-                    ok = false;
-                    break;
-                }
-                float *dst = stage0 + (size_t)slot * stage_floats;
-                const size_t src = ((size_t)pl * a.n + (cj_lo - 1)) * a.kp;
-                if (lane == 0) {
-                    mbar_arrive_expect_tx(&full[slot], 2 * bytes);
+        // ---------------- producer warp: lane 0 issues every copy ----------------
+        // Per plane: the tile's rows (plus j-halo) of both species, and the
+        // plane's density over the same rows, fetched from its 16-byte-aligned
+        // cover [a0, a0 + 4 * ceil((off + rows) / 4)) of the padded row.
+        if (lane == 0) {
+            long long g = 0;
+            bool ok = true;
+            for (int w = blockIdx.x; w < a.n_items && ok; w += gridDim.x) {
+                int cj_lo, cj_hi, ci_lo, ci_hi;
+                item_geometry(a, w, cj_lo, cj_hi, ci_lo, ci_hi);
+                const int rows = cj_hi - cj_lo + 2;
+                const uint32_t bytes = (uint32_t)(rows * a.kp * 4);
+                const int doff = (cj_lo - 1) & 3;
+                const uint32_t dbytes = has_dens ? (uint32_t)(((doff + rows + 3) & ~3) * 4) : 0u;
+                for (int pl = ci_lo - 1; pl <= ci_hi; ++pl, ++g) {
+                    const int slot = (int)(g % S);
+                    if (g >= S && !mbar_wait(&empty[slot], (uint32_t)(((g / S) - 1) & 1), a.status, 1)) {
+                        abort_flag = 1;
+                        ok = false;
+                        break;
+                    }
+                    if (abort_flag) {
+                        ok = false;
+                        break;
+                    }
+                    float *dst = stage0 + (size_t)slot * stage_floats;
+                    const size_t src = ((size_t)pl * a.n + (cj_lo - 1)) * a.kp;
+                    mbar_arrive_expect_tx(&full[slot], 2 * bytes + dbytes);
                     bulk_g2s(dst, a.pos_in + src, bytes, &full[slot]);
                     bulk_g2s(dst + spec, a.neg_in + src, bytes, &full[slot]);
+                    if (has_dens)
+                        bulk_g2s(dst + dens_off, a.dens + (size_t)pl * a.dp + (cj_lo - 1 - doff), dbytes,
+                                 &full[slot]);
                 }
-                for (int q = lane; q < rows; q += 32)
-                    dst[dens_off + q] = a.dens ? __ldg(a.dens + (size_t)pl * a.n + (cj_lo - 1) + q) : 0.f;
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&full[slot]);
             }
-        }
-        if (!ok && lane == 0) {
-            // drain: every copy still in flight must land before exit
-            for (long long gg = g - S < 0 ? 0 : g - S; gg < g; ++gg)
-                mbar_wait(&full[gg % S], (uint32_t)((gg / S) & 1), a.status, 2);
+            if (!ok) {
+                // drain: every copy still in flight must land before exit
+                for (long long gg = g - S < 0 ? 0 : g - S; gg < g; ++gg)
+                    mbar_wait(&full[gg % S], (uint32_t)((gg / S) & 1), a.status, 2);
+            }
         }
     } else {
         // ---------------- consumers ----------------
@@ -202,6 +209,7 @@ __global__ void __launch_bounds__(stream_max_threads(IPT), 1) stream_step_kernel
             const int nplanes = ci_hi - ci_lo + 2;
             const int rows_out = cj_hi - cj_lo;
             const int n_core = rows_out * ncore, n_all = rows_out * c4;
+            const int dbase = dens_off + ((cj_lo - 1) & 3);  // density of staged row q: dbase + q
             // per-slot constants: kind (0 dead, 1 core, 2 edge), row+1, vector
             int kind[IPT], rs_[IPT], c_[IPT];
             uint32_t dy2[IPT];
@@ -226,22 +234,25 @@ __global__ void __launch_bounds__(stream_max_threads(IPT), 1) stream_step_kernel
                 const int dy = 2 * (cj_lo + r) - a.two_mid;
                 dy2[k] = (uint32_t)(dy * dy);
             }
-            if (!mbar_wait(&full[g % S], (uint32_t)((g / S) & 1), a.status, 3) ||
-                !mbar_wait(&full[(g + 1) % S], (uint32_t)(((g + 1) / S) & 1), a.status, 3))
-                abort_flag = 1;
+            // ring positions of loads g (plane ci-1), g+1 (ci), g+2 (ci+1),
+            // advanced incrementally: slot index and the phase parity to wait on
+            int sm_ = (int)(g % S), sc_ = sm_ + 1 == S ? 0 : sm_ + 1, sp_ = sc_ + 1 == S ? 0 : sc_ + 1;
+            uint32_t pm_ = (uint32_t)((g / S) & 1), pc_ = sc_ == 0 ? pm_ ^ 1u : pm_, pp_ = sp_ == 0 ? pc_ ^ 1u : pc_;
+            if (!mbar_wait(&full[sm_], pm_, a.status, 3) || !mbar_wait(&full[sc_], pc_, a.status, 3)) abort_flag = 1;
             for (int q = 0; q < ci_hi - ci_lo && !abort_flag; ++q) {
-                const long long gm = g + q, gc = gm + 1, gp = gm + 2;
-                if (!mbar_wait(&full[gp % S], (uint32_t)((gp / S) & 1), a.status, 3)) {
+                if (!mbar_wait(&full[sp_], pp_, a.status, 3)) {
                     abort_flag = 1;
                     break;
                 }
-                const float *Sm = stage0 + (size_t)(gm % S) * stage_floats;
-                const float *Sc = stage0 + (size_t)(gc % S) * stage_floats;
-                const float *Sp = stage0 + (size_t)(gp % S) * stage_floats;
+                const float *Sm = stage0 + (size_t)sm_ * stage_floats;
+                const float *Sc = stage0 + (size_t)sc_ * stage_floats;
+                const float *Sp = stage0 + (size_t)sp_ * stage_floats;
                 const int ci = ci_lo + q;
                 const int dx = 2 * ci - a.two_mid;
                 const uint32_t dx2 = (uint32_t)(dx * dx);
                 const int64_t pbase = (int64_t)ci * plane_stride;
+                float *const pos_plane = a.pos_out + pbase;  // outputs of this plane; items add a 32-bit offset
+                float *const neg_plane = a.neg_out + pbase;
                 const bool edge_i = (ci == 1) || (ci == n - 2);
                 float rec_acc = 0.f, p_acc = 0.f, n_acc = 0.f;
 #pragma unroll
@@ -251,10 +262,11 @@ __global__ void __launch_bounds__(stream_max_threads(IPT), 1) stream_step_kernel
                     const int o = rs * kp + k0;
                     // convergent part: centre vectors, densities, edge shuffles
                     float4 P = lds4(Sc + o), N = lds4(Sc + spec + o);
-                    const float dens_c = Sc[dens_off + rs];
+                    const float dens_c = has_dens ? Sc[dbase + rs] : 0.f;
                     const float dcen = a.gfac * dens_c;
-                    const float dlat = a.gfac * ((Sc[dens_off + rs - 1] + Sc[dens_off + rs + 1]) +
-                                                 (Sm[dens_off + rs] + Sp[dens_off + rs]));
+                    const float dlat = has_dens ? a.gfac * ((Sc[dbase + rs - 1] + Sc[dbase + rs + 1]) +
+                                                            (Sm[dbase + rs] + Sp[dbase + rs]))
+                                                : 0.f;
                     if (kd == 1) {
                         P.x += dcen; P.y += dcen; P.z += dcen; P.w += dcen;
                         N.x += dcen; N.y += dcen; N.z += dcen; N.w += dcen;
@@ -269,19 +281,15 @@ __global__ void __launch_bounds__(stream_max_threads(IPT), 1) stream_step_kernel
                     float4 PO, NO;
                     if (kd == 1) {
                         // ---- core vector: mask-free, packed FP32x2 ----
-                        float pkm, nkm, pkp, nkp;
-                        if (lane > 0 && c > c_lo) {
-                            pkm = up_p;
-                            nkm = up_n;
-                        } else {
+                        // neighbour lane's vector when it holds the adjacent vector
+                        // of the same row, else shared memory (+ its deposition)
+                        float pkm = up_p, nkm = up_n, pkp = dn_p, nkp = dn_n;
+                        if (lane == 0 || c == c_lo) {
                             const float d = (c > c_lo || gap_below) ? dcen : 0.f;
                             pkm = Sc[o - 1] + d;
                             nkm = Sc[spec + o - 1] + d;
                         }
-                        if (lane < 31 && c < c_hi - 1) {
-                            pkp = dn_p;
-                            nkp = dn_n;
-                        } else {
+                        if (lane == 31 || c == c_hi - 1) {
                             const float d = (c < c_hi - 1 || gap_above) ? dcen : 0.f;
                             pkp = Sc[o + 4] + d;
                             nkp = Sc[spec + o + 4] + d;
@@ -374,13 +382,13 @@ __global__ void __launch_bounds__(stream_max_threads(IPT), 1) stream_step_kernel
                         NO = make_float4(no[0], no[1], no[2], no[3]);
                         const int64_t ccol = (int64_t)ci * n + cj;
                         if (c == 0) {
-                            if (scored && a.dens) t_inj.add(dens_c);
-                            if (a.dens_zero) a.dens_zero[ccol] = 0.f;
+                            if (scored && has_dens) t_inj.add(dens_c);
+                            if (a.dens_zero) a.dens_zero[(int64_t)ci * a.dp + cj] = 0.f;
                         }
                     }
-                    const int64_t out = pbase + (int64_t)cj * kp + k0;
-                    st4(a.pos_out + out, PO);
-                    st4(a.neg_out + out, NO);
+                    const int out = cj * kp + k0;
+                    st4(pos_plane + out, PO);
+                    st4(neg_plane + out, NO);
 
                     // ring columns attached to this interior column
                     const bool lo_j = (cj == 1), hi_j = (cj == n - 2);
@@ -412,7 +420,7 @@ __global__ void __launch_bounds__(stream_max_threads(IPT), 1) stream_step_kernel
                                 st4(a.neg_out + rcol * kp + k0, NO);
                             } else {
                                 float4 RP = lds4(Sr + row * kp + k0), RN = lds4(Sr + spec + row * kp + k0);
-                                const float d = a.gfac * Sr[dens_off + row];
+                                const float d = has_dens ? a.gfac * Sr[dbase + row] : 0.f;
 #pragma unroll
                                 for (int e = 0; e < 4; ++e) {
                                     const int kk = k0 + e;
@@ -423,7 +431,7 @@ __global__ void __launch_bounds__(stream_max_threads(IPT), 1) stream_step_kernel
                                 st4(a.pos_out + rcol * kp + k0, RP);
                                 st4(a.neg_out + rcol * kp + k0, RN);
                             }
-                            if (c == 0 && a.dens_zero) a.dens_zero[rcol] = 0.f;
+                            if (c == 0 && a.dens_zero) a.dens_zero[(int64_t)ri * a.dp + rj] = 0.f;
                         }
                     }
                 }
@@ -431,7 +439,12 @@ __global__ void __launch_bounds__(stream_max_threads(IPT), 1) stream_step_kernel
                 t_p.add(p_acc);
                 t_n.add(n_acc);
                 __syncwarp();
-                if (lane == 0) mbar_arrive(&empty[gm % S]);
+                if (lane == 0) mbar_arrive(&empty[sm_]);
+                // advance the window by one load
+                sm_ = sc_; pm_ = pc_;
+                sc_ = sp_; pc_ = pp_;
+                sp_ = sp_ + 1 == S ? 0 : sp_ + 1;
+                pp_ = sp_ == 0 ? pp_ ^ 1u : pp_;
             }
             if (abort_flag) break;
             __syncwarp();
@@ -460,7 +473,7 @@ static int launch_ipt(const StreamArgs &a, unsigned blocks, int threads, int sme
 }
 
 int stream_smem_bytes(int tj, int kp, int stages) {
-    return (2 * stages * 8 + 127) / 128 * 128 + stages * (2 * (tj + 2) * kp + ((tj + 2 + 3) & ~3)) * 4;
+    return (2 * stages * 8 + 127) / 128 * 128 + stages * (2 * (tj + 2) * kp + ((tj + 8) & ~3)) * 4;
 }
 
 int launch_stream_step(const pic_grid *g, const StreamShape &sh, const void *pos_in, const void *neg_in,
@@ -485,6 +498,7 @@ int launch_stream_step(const pic_grid *g, const StreamShape &sh, const void *pos
     a.nze = (int)g->nze;
     a.gap_end = (int)(g->nze + g->no_z);
     a.reflecting = g->wall == PIC_WALL_REFLECTING;
+    a.dp = (int)dens_pitch(g->no_xy);
     a.tj = sh.tile_rows;
     a.li = sh.planes_per_item;
     a.jt = (a.n - 2 + a.tj - 1) / a.tj;

@@ -184,8 +184,10 @@ def run(config, mode: str = "serial", rng=None, max_steps=None, alpha_cm3_s=None
     I = 0.0
     R = 0.0
     snap = None
+    step_wall = np.zeros(last)
     t0 = time.perf_counter()
     for step in range(last):
+        ts = time.perf_counter()
         inj = 0.0
         m = int(sched[step])
         if m > 0:
@@ -226,12 +228,13 @@ def run(config, mode: str = "serial", rng=None, max_steps=None, alpha_cm3_s=None
                 pos, pos_next = pos_next, pos
                 neg, neg_next = neg_next, neg
         f_t[step] = 1.0 if I == 0.0 else (I - R) / I
+        step_wall[step] = time.perf_counter() - ts
         if snapshot_step is not None and step == snapshot_step:
             snap = (pos.copy(), neg.copy())
     wall = time.perf_counter() - t0
     ks = float("nan") if last < total else 1.0 / f_t[-1]
     res = dict(f_t=f_t, ks=ks, injected=injected, recombined=recombined, n_positive=n_pos, n_negative=n_neg,
-               track_density_xy=td, steps=last, wall_s=wall)
+               track_density_xy=td, steps=last, wall_s=wall, step_wall_s=step_wall)
     if snap is not None:
         res["positive"], res["negative"] = snap
     elif keep_fields:

@@ -61,6 +61,7 @@ def test_host_only_calls_without_a_gpu(lib):
     assert lib.pic_kpitch(406) == 408
     assert lib.pic_kpitch(408) == 408
     assert lib.pic_kpitch(3) == 8
+    assert lib.pic_dens_pitch(1068) == 1068 and lib.pic_dens_pitch(25) == 28
 
 
 def test_invalid_grid_is_refused_before_any_device_work(lib):
