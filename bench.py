@@ -51,6 +51,8 @@ WORKLOADS = {
     "full_electrode_5um": ("5 um full electrode, r=0.265 cm, 1068x1068x406, 10 pulses, seed 1",
                            dict(BEAM, grid_size_um=5.0, sampled_radius_cm=0.265, n_pulses=10, seed=1,
                                 max_voxels=2e9)),
+    "column_5um_r15": ("5 um column, r=0.15 cm, 608x608x406, 8.91 Gy/s, seed 1 (profiling size: 2.4 GB of fields)",
+                       dict(BEAM, grid_size_um=5.0, sampled_radius_cm=0.15, seed=1, max_voxels=2e9)),
     "column_5um_r05": ("5 um column, r=0.05 cm, 208x208x406, 8.91 Gy/s, seed 1",
                        dict(BEAM, grid_size_um=5.0, sampled_radius_cm=0.05, seed=1, max_voxels=2e9)),
     "column_10um_r008": ("10 um column, r=0.008 cm, 24x24x206, seed 1",
@@ -335,7 +337,7 @@ def run_gb300(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=600)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="full_electrode_5um")
