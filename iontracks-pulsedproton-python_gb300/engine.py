@@ -181,32 +181,47 @@ class ChamberEngine:
         self.parity = (self.parity + n_steps) & 1
         self.step_index += n_steps
 
-    def graph(self, key, track_offsets: np.ndarray, tally_row: int, stream=None):
-        """A CUDA graph of one segment, created once per key and replayed.
+    def run_segment_graphed(self, key, track_offsets: np.ndarray, track_base: int = 0, stream=None) -> None:
+        """Same as :meth:`run_segment`, replayed from a CUDA graph.
 
-        The graph bakes in the buffers, the field and density parities and
-        the tally row, so the key must capture all of them."""
-        if key in self._graphs:
-            return self._graphs[key]
+        The first call with a key captures the segment's launches into a
+        graph; later calls with the same key replay it. A graph bakes in the
+        buffers, the track offsets and base, and the field and density
+        parities, so the key must determine all of them (the caller's job);
+        the parities are checked here. Tallies go to a staging block owned by
+        the graph and are copied to the run's tally rows after each replay.
+        """
         off = np.ascontiguousarray(track_offsets, dtype=np.int64)
         n_steps = len(off) - 1
-        g = self.grid
-        h = ctypes.c_void_p()
+        if n_steps <= 0:
+            return
+        row = self.step_index
+        if row + n_steps > self.tally.shape[0]:
+            raise ValueError("tally buffer too small for this segment")
+        if track_base < 0 or track_base + off[-1] > self.xs.numel():
+            raise ValueError("track offsets exceed the uploaded track buffer")
         st = self._stream(stream)
-        rc = self.lib.pic_graph_create(
-            ctypes.byref(g), self.pos[0].data_ptr(), self.neg[0].data_ptr(), self.pos[1].data_ptr(),
-            self.neg[1].data_ptr(), self.parity, n_steps, self.xs.data_ptr(), self.ys.data_ptr(),
-            off.ctypes.data_as(ctypes.c_void_p), self.dens[0].data_ptr(), self.dens[1].data_ptr(),
-            self.step_index & 1, self.counts.data_ptr(), self.tally[tally_row].data_ptr(),
-            self.workspace.data_ptr(), self.workspace.numel(), st, ctypes.byref(h),
-        )
-        N.check(rc, "pic_graph_create")
-        self._graphs[key] = (h.value, n_steps)
-        return self._graphs[key]
-
-    def launch_graph(self, key, stream=None) -> None:
-        handle, n_steps = self._graphs[key]
-        N.check(self.lib.pic_graph_launch(handle, self._stream(stream)), "pic_graph_launch")
+        entry = self._graphs.get(key)
+        if entry is None:
+            torch = self.torch
+            stage = torch.zeros((n_steps, 4), dtype=torch.float64, device=self.device)
+            g = self.grid
+            h = ctypes.c_void_p()
+            rc = self.lib.pic_graph_create(
+                ctypes.byref(g), self.pos[0].data_ptr(), self.neg[0].data_ptr(), self.pos[1].data_ptr(),
+                self.neg[1].data_ptr(), self.parity, n_steps, self.xs.data_ptr() + 8 * int(track_base),
+                self.ys.data_ptr() + 8 * int(track_base), off.ctypes.data_as(ctypes.c_void_p),
+                self.dens[0].data_ptr(), self.dens[1].data_ptr(), self.step_index & 1, self.counts.data_ptr(),
+                stage.data_ptr(), self.workspace.data_ptr(), self.workspace.numel(), st, ctypes.byref(h),
+            )
+            N.check(rc, "pic_graph_create")
+            entry = (h.value, n_steps, stage, self.parity, self.step_index & 1)
+            self._graphs[key] = entry
+        handle, n, stage, parity, dparity = entry
+        if n != n_steps or parity != self.parity or dparity != (self.step_index & 1):
+            raise RuntimeError("graph key reused for a segment with a different length or parity")
+        N.check(self.lib.pic_graph_launch(handle, st), "pic_graph_launch")
+        self.tally[row : row + n_steps].copy_(stage)
         self.parity = (self.parity + n_steps) & 1
         self.step_index += n_steps
 
@@ -220,8 +235,8 @@ class ChamberEngine:
             raise RuntimeError(f"a fused-step kernel gave up on a bounded wait (code {st.value}); results are invalid")
 
     def close(self) -> None:
-        for h, _ in self._graphs.values():
-            self.lib.pic_graph_destroy(h)
+        for entry in self._graphs.values():
+            self.lib.pic_graph_destroy(entry[0])
         self._graphs.clear()
 
     def __del__(self):

@@ -67,6 +67,8 @@ def run_simulation_b200(
     alpha_cm3_s: Optional[float] = None,
     chunk_steps: int = 256,
     shape: Optional[dict] = None,
+    use_graphs: Optional[bool] = None,
+    tune: bool = False,
 ):
     """Simulate a pulse train on one GB300 and return the reference's Result.
 
@@ -77,7 +79,12 @@ def run_simulation_b200(
     ``return_fields=False`` returns empty field arrays. ``alpha_cm3_s``
     overrides the recombination coefficient. ``shape`` overrides the fused
     step's launch shape (``variant`` "flat"/"stream", ``tile_rows``, ...);
-    by default the library chooses.
+    by default the library chooses, or with ``tune=True`` the autotuner
+    (timed once per grid and cached). ``use_graphs`` replays each chunk of
+    ``chunk_steps`` steps from a CUDA graph captured once (every pulse has
+    the same per-step track counts, so a pulse's chunks replay for every
+    pulse); by default graphs are used for grids under 30 M voxels, where
+    launch overhead is a visible part of a step.
     """
     if dtype not in ("float32", "float64"):
         raise ValueError(f"dtype must be 'float32' or 'float64', got {dtype!r}")
@@ -91,6 +98,12 @@ def run_simulation_b200(
 
     eng = ChamberEngine(config, dtype=dtype, alpha_cm3_s=alpha_cm3_s, max_tracks=max_pulse_tracks, shape=shape)
     torch = eng.torch
+    if tune and not shape:
+        from .autotune import tune as _tune
+
+        _tune(eng, quick=True)
+    if use_graphs is None:
+        use_graphs = int(config.no_xy) ** 2 * int(config.no_z_with_buffer) < 30_000_000
     diagnostics = Diagnostics(config)
     report_every = max(1, total // 20)
     loop_t0 = perf_counter()
@@ -113,7 +126,13 @@ def run_simulation_b200(
         while c0 < s1 - s0:
             c1 = min(c0 + chunk_steps, s1 - s0)
             seg = offsets[c0 : c1 + 1] - offsets[c0]
-            eng.run_segment(seg, track_base=int(offsets[c0]))
+            if use_graphs:
+                # the same chunk of every pulse (or of every idle stretch) has
+                # the same offsets; the parities complete the key
+                key = (with_tracks, c0 if with_tracks else -1, c1 - c0, eng.parity, eng.step_index & 1)
+                eng.run_segment_graphed(key, seg, track_base=int(offsets[c0]))
+            else:
+                eng.run_segment(seg, track_base=int(offsets[c0]))
             steps_done = s0 + c1
             if progress and (steps_done // report_every) != ((s0 + c0) // report_every):
                 print(f"  step {steps_done}/{total}")

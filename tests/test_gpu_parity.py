@@ -237,3 +237,20 @@ def test_stream_fields_mid_run_match_the_oracle(oracle):
     np.testing.assert_allclose(res.positive_array, ref["positive"], rtol=0, atol=peak * 1e-5)
     np.testing.assert_allclose(res.negative_array, ref["negative"], rtol=0, atol=peak * 1e-5)
     assert res.recombination[:k + 1].sum() == pytest.approx(ref["recombined"][:k + 1].sum(), rel=TALLY_REL)
+
+
+@pytest.mark.parametrize("dtype", ["float32", "float64"])
+def test_graph_replay_matches_direct_launches(oracle, dtype):
+    """Chunks replayed from CUDA graphs (captured once, replayed for every
+    pulse and idle stretch with the same parities) give the same run as
+    launching every step directly."""
+    cfg = make_config("fast_dense", n_pulses=4, repetition_rate_hz=20000.0)
+    a = _solver()(cfg, progress=False, use_graphs=False, chunk_steps=3, dtype=dtype)
+    b = _solver()(cfg, progress=False, use_graphs=True, chunk_steps=3, dtype=dtype)
+    np.testing.assert_array_equal(a.track_density_xy, b.track_density_xy)
+    tol = 1e-6 if dtype == "float32" else 1e-12
+    np.testing.assert_allclose(b.recombination, a.recombination, rtol=tol, atol=tol * np.abs(a.recombination).max())
+    np.testing.assert_allclose(b.n_positive, a.n_positive, rtol=tol, atol=tol * np.abs(a.n_positive).max())
+    assert b.ks == pytest.approx(a.ks, rel=tol)
+    ref = oracle.run(cfg, mode="batched", threads=2)
+    assert abs(b.ks - ref["ks"]) <= (KS_ABS if dtype == "float32" else 1e-10)
