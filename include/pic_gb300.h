@@ -204,6 +204,67 @@ int pic_graph_create(const pic_grid *g, void *pos0, void *neg0, void *pos1, void
 int pic_graph_launch(uintptr_t graph, uintptr_t stream);
 int pic_graph_destroy(uintptr_t graph);
 
+/*
+ * Batched runs: many independent grids advanced together.
+ *
+ * Each grid occupies its own block of packed device buffers, described by a
+ * pic_batch_cfg entry (its pic_grid scalars -- launch-shape fields ignored --
+ * and its offsets). One global step advances every active grid by one of its
+ * own time steps, with two launches for the whole batch: a deposition over
+ * the step's tracks of all grids (a task list maps warps to grids and
+ * tracks) and the flat fused step over a work table that gives each block
+ * one grid and a contiguous range of that grid's items (a grid's blocks are
+ * consecutive; its last block to finish writes its tallies). Grids that have
+ * finished are left out of the work table and task list of later steps.
+ *
+ * Replaces running the reference's driver once per configuration
+ * (run_simulation_numba, solver_numba.py:237-370) for a parameter sweep.
+ */
+typedef struct pic_batch_cfg {
+    int64_t field_off;  /* element offset of the grid's [no_xy][no_xy][kpitch] fields    */
+    int64_t dens_off;   /* element offset of its [no_xy][dens_pitch] density           */
+    int64_t counts_off; /* offset of its [no_xy][no_xy] track histogram                */
+    int64_t tally_off;  /* row offset of its [steps][4] tallies                         */
+    pic_grid grid;      /* the grid's scalars (dtype must match the batch)             */
+} pic_batch_cfg;
+
+typedef struct pic_batch_launch {
+    const pic_batch_cfg *cfgs;             /* device, n_cfgs entries                         */
+    int32_t n_cfgs;
+    int32_t dtype;                         /* PIC_F32 or PIC_F64, for every grid             */
+    const int32_t *blk_cfg;                /* device, per block: its grid                    */
+    const int64_t *blk_item0, *blk_item1;  /* device, per block: its item range              */
+    int32_t n_blocks;
+    int32_t reserved;
+    const int32_t *cfg_blk0, *cfg_nblk;    /* device, per grid: first block, block count     */
+    void *pos[2], *neg[2];                 /* device, packed fields of time levels 0 and 1   */
+    void *dens[2];                         /* device, packed densities, by step parity       */
+    const double *xs, *ys;                 /* device, packed track centres                   */
+    const int32_t *task_cfg;               /* device, per task (grid, tracks of one step):   */
+    const int64_t *task_first;             /*   grid, first track, and first warp within the */
+    const int64_t *task_prefix;            /*   step's deposition launch                     */
+    const int64_t *step_task_off;          /* host, n_steps + 1: the steps' task ranges      */
+    const int64_t *step_tracks;            /* host, n_steps: tracks deposited in each step   */
+    int64_t first_step, n_steps;           /* global steps [first_step, first_step+n_steps)  */
+    uint32_t *counts;                      /* device, packed track histograms                */
+    double *tally;                         /* device, packed [rows][4] tallies               */
+    void *workspace;                       /* device, pic_batched_workspace_bytes, zeroed    */
+    int64_t workspace_bytes;
+} pic_batch_launch;
+
+/* Workspace of a batched launch with n_blocks blocks and n_cfgs grids. */
+int pic_batched_workspace_bytes(int32_t n_blocks, int32_t n_cfgs, int64_t *bytes);
+
+/* Runs global steps [first_step, first_step + n_steps) of a batch. Step s
+ * reads time level s & 1 and density buffer s & 1, writes level (s+1) & 1
+ * and clears density buffer (s+1) & 1; both density buffers must be zero
+ * before step 0. */
+int pic_batched_segment(const pic_batch_launch *launch, uintptr_t stream);
+
+/* The same launches captured into a CUDA graph (replay with
+ * pic_graph_launch, free with pic_graph_destroy). */
+int pic_batched_graph_create(const pic_batch_launch *launch, uintptr_t stream, uintptr_t *graph_out);
+
 #ifdef __cplusplus
 }
 #endif

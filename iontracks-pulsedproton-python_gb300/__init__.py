@@ -25,6 +25,8 @@ __all__ = [
     "CylinderSampler",
     "build_track_schedule",
     "run_simulation_b200",
+    "run_batched_b200",
+    "saturation_sweep_configs",
 ]
 
 
@@ -35,4 +37,8 @@ def __getattr__(name):
         from .solver_b200 import run_simulation_b200
 
         return run_simulation_b200
+    if name in ("run_batched_b200", "saturation_sweep_configs"):
+        from . import batched
+
+        return getattr(batched, name)
     raise AttributeError(name)

@@ -1,0 +1,316 @@
+"""Batched runs: many independent chamber configurations on one GB300 at once.
+
+``run_batched_b200(configs)`` returns one reference :class:`Result` per
+configuration -- the same results ``run_simulation_b200`` gives for each of
+them alone -- but advances all grids together: each global step is one
+deposition launch over the step's tracks of every grid and one fused-step
+launch over every active grid (``pic_batched_segment``). The grids may differ
+in every respect: size, voltage and gap (hence time step and coefficients),
+dose rate, pulse length, step count, wall, seed.
+
+``saturation_sweep_configs()`` builds the 64-configuration saturation sweep:
+voltages log-spaced over 25-400 V, gaps of 0.1/0.2/0.3 cm, dose rates
+log-uniform over 1-100 Gy/s, pulse lengths 100-1000 us at 50 Hz, 5 or 10 um
+voxels with sampled radii 0.008-0.03 cm, seeds 1-64, the random choices drawn
+from a fixed meta-seed.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import warnings
+from time import perf_counter
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _native as N
+from .config import SimulationConfig
+from .engine import make_grid
+from .pulses import TrackSampler, build_track_schedule
+from .state import Diagnostics, collection_efficiency
+
+ITEMS_PER_BLOCK = 256 * 8
+
+
+class PicBatchCfg(ctypes.Structure):
+    _fields_ = [
+        ("field_off", ctypes.c_int64),
+        ("dens_off", ctypes.c_int64),
+        ("counts_off", ctypes.c_int64),
+        ("tally_off", ctypes.c_int64),
+        ("grid", N.PicGrid),
+    ]
+
+
+class PicBatchLaunch(ctypes.Structure):
+    _fields_ = [
+        ("cfgs", ctypes.c_void_p),
+        ("n_cfgs", ctypes.c_int32),
+        ("dtype", ctypes.c_int32),
+        ("blk_cfg", ctypes.c_void_p),
+        ("blk_item0", ctypes.c_void_p),
+        ("blk_item1", ctypes.c_void_p),
+        ("n_blocks", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("cfg_blk0", ctypes.c_void_p),
+        ("cfg_nblk", ctypes.c_void_p),
+        ("pos", ctypes.c_void_p * 2),
+        ("neg", ctypes.c_void_p * 2),
+        ("dens", ctypes.c_void_p * 2),
+        ("xs", ctypes.c_void_p),
+        ("ys", ctypes.c_void_p),
+        ("task_cfg", ctypes.c_void_p),
+        ("task_first", ctypes.c_void_p),
+        ("task_prefix", ctypes.c_void_p),
+        ("step_task_off", ctypes.c_void_p),
+        ("step_tracks", ctypes.c_void_p),
+        ("first_step", ctypes.c_int64),
+        ("n_steps", ctypes.c_int64),
+        ("counts", ctypes.c_void_p),
+        ("tally", ctypes.c_void_p),
+        ("workspace", ctypes.c_void_p),
+        ("workspace_bytes", ctypes.c_int64),
+    ]
+
+
+def _align(x: int, a: int = 64) -> int:
+    return (x + a - 1) // a * a
+
+
+def saturation_sweep_configs(n: int = 64, meta_seed: int = 20260527, **overrides) -> list:
+    """The batched saturation sweep (see the module docstring)."""
+    rng = np.random.default_rng(meta_seed)
+    volts = np.logspace(np.log10(25.0), np.log10(400.0), n)
+    out = []
+    for i in range(n):
+        kw = dict(
+            E_MeV_u=56.2,
+            voltage_V=float(volts[i]),
+            electrode_gap_cm=float(rng.choice([0.1, 0.2, 0.3])),
+            dose_rate_Gy_s=float(10.0 ** rng.uniform(0.0, 2.0)),
+            pulse_duration_s=float(rng.uniform(100e-6, 1000e-6)),
+            repetition_rate_hz=50.0,
+            grid_size_um=float(rng.choice([5.0, 10.0])),
+            sampled_radius_cm=float(rng.uniform(0.008, 0.03)),
+            seed=i + 1,
+            max_voxels=2e9,
+        )
+        kw.update(overrides)
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            out.append(SimulationConfig(**kw))
+    return out
+
+
+def _phases(total_steps: Sequence[int]):
+    """Intervals [s0, s1) of global steps over which the set of active grids
+    (those with s < total_steps) is constant, with that set."""
+    ends = sorted(set(int(t) for t in total_steps))
+    phases = []
+    s0 = 0
+    for e in ends:
+        if e <= s0:
+            continue
+        active = [c for c, t in enumerate(total_steps) if t > s0]
+        phases.append((s0, e, active))
+        s0 = e
+    return phases
+
+
+def run_batched_b200(
+    configs: Sequence,
+    rngs: Optional[Sequence[np.random.Generator]] = None,
+    return_fields: bool = False,
+    dtype: str = "float32",
+    alpha_cm3_s: Optional[float] = None,
+    chunk_steps: int = 512,
+    progress: bool = False,
+):
+    """Simulate every configuration and return their Results, in order.
+
+    Equivalent to ``[run_simulation_b200(c) for c in configs]`` (same tracks,
+    same tallies to float32 rounding) but with all grids advanced together.
+    """
+    import torch
+
+    if not torch.cuda.is_available():
+        raise RuntimeError("run_batched_b200 needs a CUDA device (a GB300); none is visible")
+    lib = N.load()
+    N.device_info()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    n_cfg = len(configs)
+    if n_cfg == 0:
+        return []
+    tdt = torch.float32 if dtype == "float32" else torch.float64
+    es = 4 if dtype == "float32" else 8
+    grids = [make_grid(c, dtype, alpha_cm3_s) for c in configs]
+    totals = [int(c.total_time_steps) for c in configs]
+
+    # --- tracks of every grid, sampled on the host (same stream as the reference)
+    rngs = rngs if rngs is not None else [np.random.default_rng(c.seed) for c in configs]
+    xs_parts, ys_parts, offsets = [], [], []
+    track_base = []
+    base = 0
+    for c, rng in zip(configs, rngs):
+        sched = build_track_schedule(c, rng)
+        n_tr = int(sched.sum())
+        xs, ys = TrackSampler(rng, c.mid_xy, c.sampling_radius, c.no_xy).sample(n_tr)
+        off = np.zeros(len(sched) + 1, dtype=np.int64)
+        np.cumsum(sched, out=off[1:])
+        xs_parts.append(xs)
+        ys_parts.append(ys)
+        offsets.append(off)
+        track_base.append(base)
+        base += n_tr
+
+    # --- packed layout
+    field_off, dens_off, counts_off, tally_off = [], [], [], []
+    fo = do = co = to = 0
+    items = []
+    for g, t in zip(grids, totals):
+        n, kp = int(g.no_xy), int(g.kpitch)
+        dp = (n + 3) // 4 * 4
+        field_off.append(fo)
+        dens_off.append(do)
+        counts_off.append(co)
+        tally_off.append(to)
+        fo = _align(fo + n * n * kp)
+        do = _align(do + n * dp)
+        co = _align(co + n * n)
+        to += t
+        items.append(n * n * (kp // 4))
+    need = 4 * fo * es + 2 * do * es + co * 4 + to * 32 + 16 * base
+    free, _ = torch.cuda.mem_get_info(dev)
+    if need > 0.9 * free:
+        raise MemoryError(f"batch needs {need / 2**30:.2f} GiB of device memory, {free / 2**30:.2f} GiB free")
+
+    cfg_arr = (PicBatchCfg * n_cfg)()
+    for c in range(n_cfg):
+        cfg_arr[c].field_off, cfg_arr[c].dens_off = field_off[c], dens_off[c]
+        cfg_arr[c].counts_off, cfg_arr[c].tally_off = counts_off[c], tally_off[c]
+        cfg_arr[c].grid = grids[c]
+    cfg_dev = torch.frombuffer(bytearray(cfg_arr), dtype=torch.uint8).to(dev)
+
+    kw = dict(device=dev)
+    pos = [torch.zeros(max(fo, 1), dtype=tdt, **kw) for _ in range(2)]
+    neg = [torch.zeros(max(fo, 1), dtype=tdt, **kw) for _ in range(2)]
+    dens = [torch.zeros(max(do, 1), dtype=tdt, **kw) for _ in range(2)]
+    counts = torch.zeros(max(co, 1), dtype=torch.int32, **kw)
+    tally = torch.zeros((max(to, 1), 4), dtype=torch.float64, **kw)
+    xs_dev = torch.from_numpy(np.concatenate(xs_parts) if base else np.zeros(1)).to(dev)
+    ys_dev = torch.from_numpy(np.concatenate(ys_parts) if base else np.zeros(1)).to(dev)
+
+    # --- per global step: tasks (grid, first track, first warp)
+    S = max(totals)
+    t_cfg, t_first, t_prefix = [], [], []
+    step_task_off = np.zeros(S + 1, dtype=np.int64)
+    step_tracks = np.zeros(S, dtype=np.int64)
+    counts_by_cfg = [np.diff(o) for o in offsets]
+    for s in range(S):
+        w = 0
+        for c in range(n_cfg):
+            if s < totals[c]:
+                m = int(counts_by_cfg[c][s])
+                if m > 0:
+                    t_cfg.append(c)
+                    t_first.append(track_base[c] + int(offsets[c][s]))
+                    t_prefix.append(w)
+                    w += m
+        step_tracks[s] = w
+        step_task_off[s + 1] = len(t_cfg)
+    task_cfg = torch.tensor(t_cfg if t_cfg else [0], dtype=torch.int32, device=dev)
+    task_first = torch.tensor(t_first if t_first else [0], dtype=torch.int64, device=dev)
+    task_prefix = torch.tensor(t_prefix if t_prefix else [0], dtype=torch.int64, device=dev)
+
+    # --- work tables, one per set of active grids
+    phases = []
+    max_blocks = 1
+    for s0, s1, active in _phases(totals):
+        blk_cfg, i0, i1 = [], [], []
+        cfg_blk0 = np.zeros(n_cfg, dtype=np.int32)
+        cfg_nblk = np.zeros(n_cfg, dtype=np.int32)
+        for c in active:
+            nb = max(1, -(-items[c] // ITEMS_PER_BLOCK))
+            cfg_blk0[c] = len(blk_cfg)
+            cfg_nblk[c] = nb
+            for b in range(nb):
+                blk_cfg.append(c)
+                i0.append(b * items[c] // nb)
+                i1.append((b + 1) * items[c] // nb)
+        max_blocks = max(max_blocks, len(blk_cfg))
+        phases.append((s0, s1, dict(
+            blk_cfg=torch.tensor(blk_cfg, dtype=torch.int32, device=dev),
+            blk_item0=torch.tensor(i0, dtype=torch.int64, device=dev),
+            blk_item1=torch.tensor(i1, dtype=torch.int64, device=dev),
+            cfg_blk0=torch.from_numpy(cfg_blk0).to(dev),
+            cfg_nblk=torch.from_numpy(cfg_nblk).to(dev),
+            n_blocks=len(blk_cfg),
+        )))
+    wsb = ctypes.c_int64()
+    N.check(lib.pic_batched_workspace_bytes(max_blocks, n_cfg, ctypes.byref(wsb)), "pic_batched_workspace_bytes")
+    workspace = torch.zeros(int(wsb.value), dtype=torch.uint8, device=dev)
+
+    st = torch.cuda.current_stream(dev).cuda_stream
+    t0 = perf_counter()
+    for s0, s1, tab in phases:
+        c0 = s0
+        while c0 < s1:
+            c1 = min(c0 + chunk_steps, s1)
+            L = PicBatchLaunch()
+            L.cfgs = cfg_dev.data_ptr()
+            L.n_cfgs = n_cfg
+            L.dtype = N.PIC_F32 if dtype == "float32" else N.PIC_F64
+            L.blk_cfg = tab["blk_cfg"].data_ptr()
+            L.blk_item0 = tab["blk_item0"].data_ptr()
+            L.blk_item1 = tab["blk_item1"].data_ptr()
+            L.n_blocks = tab["n_blocks"]
+            L.cfg_blk0 = tab["cfg_blk0"].data_ptr()
+            L.cfg_nblk = tab["cfg_nblk"].data_ptr()
+            L.pos[0], L.pos[1] = pos[0].data_ptr(), pos[1].data_ptr()
+            L.neg[0], L.neg[1] = neg[0].data_ptr(), neg[1].data_ptr()
+            L.dens[0], L.dens[1] = dens[0].data_ptr(), dens[1].data_ptr()
+            L.xs, L.ys = xs_dev.data_ptr(), ys_dev.data_ptr()
+            L.task_cfg, L.task_first, L.task_prefix = task_cfg.data_ptr(), task_first.data_ptr(), task_prefix.data_ptr()
+            sto = np.ascontiguousarray(step_task_off[c0 : c1 + 1])
+            stt = np.ascontiguousarray(step_tracks[c0:c1])
+            L.step_task_off = sto.ctypes.data
+            L.step_tracks = stt.ctypes.data
+            L.first_step, L.n_steps = c0, c1 - c0
+            L.counts, L.tally = counts.data_ptr(), tally.data_ptr()
+            L.workspace, L.workspace_bytes = workspace.data_ptr(), workspace.numel()
+            N.check(lib.pic_batched_segment(ctypes.byref(L), st), "pic_batched_segment")
+            if progress:
+                print(f"  global step {c1}/{S}")
+            c0 = c1
+    torch.cuda.synchronize(dev)
+    elapsed = perf_counter() - t0
+
+    # --- one Result per configuration
+    tally_h = tally.cpu().numpy()
+    counts_h = counts.cpu().numpy().view(np.uint32)
+    results = []
+    pos_h = neg_h = None
+    if return_fields:
+        pos_h = [pos[0].cpu().numpy(), pos[1].cpu().numpy()]
+        neg_h = [neg[0].cpu().numpy(), neg[1].cpu().numpy()]
+    for c, cfg in enumerate(configs):
+        diag = Diagnostics(cfg)
+        diag.record_block(0, tally_h[tally_off[c] : tally_off[c] + totals[c]])
+        n = int(cfg.no_xy)
+        diag.track_density_xy = counts_h[counts_off[c] : counts_off[c] + n * n].reshape(n, n).astype(np.float64)
+        f_t = collection_efficiency(diag.injected, diag.recombined, totals[c])
+        time_s = (np.arange(totals[c]) + 1) * cfg.dt
+        ks = 1.0 / f_t[-1]
+        if return_fields:
+            lvl = totals[c] & 1
+            kp = int(grids[c].kpitch)
+            sl = slice(field_off[c], field_off[c] + n * n * kp)
+            p = pos_h[lvl][sl].reshape(n, n, kp)[:, :, : int(cfg.no_z_with_buffer)].astype(np.float64)
+            q = neg_h[lvl][sl].reshape(n, n, kp)[:, :, : int(cfg.no_z_with_buffer)].astype(np.float64)
+        else:
+            p = q = np.zeros((0, 0, 0))
+        res = diag.build_result(cfg, time_s, f_t, ks, p, q)
+        res.loop_elapsed_s = elapsed
+        results.append(res)
+    return results

@@ -1,0 +1,192 @@
+// batched.cu -- many independent chamber configurations advanced together.
+//
+// The grids of a batch live at their own offsets in packed buffers (fields,
+// 2D densities, track histograms, tallies), described by a device table of
+// pic_batch_cfg entries (each grid's pic_grid scalars and offsets). One global
+// step advances every active grid by one of its own time steps with two
+// launches for the whole batch:
+//   * batched_deposit_kernel -- one warp per track of this step, over the
+//     tracks of every grid (a task list maps warp -> grid, track);
+//   * batched_step_kernel -- the flat fused step (pic_flat.cuh) over a work
+//     table that gives each block one grid and a contiguous range of that
+//     grid's items; a grid's blocks are consecutive in the table, and the
+//     last of them to finish (per-grid completion counter) writes the grid's
+//     tallies for this step.
+// Grids differ in size, time step, coefficients, step count and schedule; a
+// grid that has finished is simply absent from the work table and the task
+// list of later steps (the caller builds one table per set of active grids).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "pic_deposit.cuh"
+#include "pic_device.cuh"
+#include "pic_flat.cuh"
+#include "pic_internal.h"
+
+namespace pic {
+
+template <typename T>
+struct BatchStepArgs {
+    const pic_batch_cfg *cfgs;
+    const int32_t *blk_cfg;
+    const int64_t *blk_item0, *blk_item1;
+    const int32_t *cfg_blk0, *cfg_nblk;
+    const T *pos_in, *neg_in;
+    T *pos_out, *neg_out;
+    const T *dens;    // packed density buffer of this step
+    T *dens_zero;     // packed buffer of the next step, cleared here
+    double *tally;    // packed [rows][4]
+    double *partials; // [n_blocks][4]
+    unsigned int *counters;  // [n_cfgs]
+    int64_t step;     // global step index (row within each grid's tallies)
+};
+
+template <typename T>
+__device__ void grid_args(const pic_batch_cfg &C, const BatchStepArgs<T> &b, StepArgs<T> &a) {
+    const pic_grid &g = C.grid;
+    a.pos_in = b.pos_in + C.field_off;
+    a.neg_in = b.neg_in + C.field_off;
+    a.pos_out = b.pos_out + C.field_off;
+    a.neg_out = b.neg_out + C.field_off;
+    a.dens = b.dens + C.dens_off;
+    a.dens_zero = b.dens_zero + C.dens_off;
+    a.n = g.no_xy;
+    a.kp = g.kpitch;
+    a.c4 = g.kpitch / 4;
+    a.items = g.no_xy * g.no_xy * a.c4;
+    a.dp = (g.no_xy + 3) / 4 * 4;
+    a.nzb = (int)g.nzb;
+    a.nze = (int)g.nze;
+    a.gap_end = (int)(g.nze + g.no_z);
+    a.reflecting = g.wall == PIC_WALL_REFLECTING;
+    a.p_lat = (T)g.p_lat; a.p_zm = (T)g.p_zm; a.p_zp = (T)g.p_zp; a.p_cen = (T)g.p_cen;
+    a.n_lat = (T)g.n_lat; a.n_zm = (T)g.n_zm; a.n_zp = (T)g.n_zp; a.n_cen = (T)g.n_cen;
+    a.alpha_dt = (T)g.alpha_dt;
+    a.gfac = (T)g.gaussian_factor;
+    a.score.two_mid = (int64_t)(2.0 * g.mid_xy);
+    const double r4 = 4.0 * g.scoring_radius_sq;
+    a.score.thr4 = r4 >= 4.0e18 ? (int64_t)4.0e18 : (int64_t)ceil(r4) - 1;
+    a.injected_scale = g.gaussian_factor * (double)g.no_z;
+}
+
+template <typename T, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) batched_step_kernel(BatchStepArgs<T> b) {
+    __shared__ double red[BLOCK / 32][4];
+    __shared__ bool last;
+    // the block's grid arguments, staged once in shared memory and read by
+    // broadcast (keeps them out of the registers of every thread)
+    __shared__ StepArgs<T> a;
+    const int blk = blockIdx.x;
+    const int c = b.blk_cfg[blk];
+    const pic_batch_cfg &C = b.cfgs[c];
+    if (threadIdx.x == 0) grid_args(C, b, a);
+    __syncthreads();
+    Tally<T> t_rec, t_p, t_n, t_inj;
+    const int64_t i1 = b.blk_item1[blk];
+    for (int64_t item = b.blk_item0[blk] + threadIdx.x; item < i1; item += BLOCK)
+        flat_item(a, item, t_rec, t_p, t_n, t_inj);
+    double v[4] = {t_inj.value(), t_rec.value(), t_p.value(), t_n.value()};
+    block_sum4<BLOCK>(v, red);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) b.partials[4 * (int64_t)blk + q] = v[q];
+        __threadfence();
+        last = (atomicAdd(b.counters + c, 1u) == (unsigned)b.cfg_nblk[c] - 1u);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const int b0 = b.cfg_blk0[c], nb = b.cfg_nblk[c];
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int k = threadIdx.x; k < nb; k += BLOCK)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[q] += __ldcg(b.partials + 4 * (int64_t)(b0 + k) + q);
+    block_sum4<BLOCK>(acc, red);
+    if (threadIdx.x == 0) {
+        double *t = b.tally + 4 * (C.tally_off + b.step);
+        t[0] = acc[0] * a.injected_scale;
+        t[1] = acc[1];
+        t[2] = acc[2];
+        t[3] = acc[3];
+        b.counters[c] = 0u;
+        __threadfence();
+    }
+}
+
+template <typename T, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) batched_deposit_kernel(const pic_batch_cfg *cfgs,
+                                                                      const int32_t *task_cfg,
+                                                                      const int64_t *task_first,
+                                                                      const int64_t *task_prefix, int n_tasks,
+                                                                      int64_t total, const double *xs,
+                                                                      const double *ys, T *dens, uint32_t *counts) {
+    const int64_t w = (int64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
+    if (w >= total) return;
+    // last task whose first warp is <= w
+    int lo = 0, hi = n_tasks - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (task_prefix[mid] <= w) lo = mid; else hi = mid - 1;
+    }
+    const pic_batch_cfg &C = cfgs[task_cfg[lo]];
+    const int64_t idx = task_first[lo] + (w - task_prefix[lo]);
+    const int64_t n = C.grid.no_xy;
+    deposit_track<T>(xs[idx], ys[idx], n, (n + 3) / 4 * 4, C.grid.cutoff_voxels, (T)C.grid.h2_over_b2,
+                     dens + C.dens_off, counts + C.counts_off, threadIdx.x & 31);
+}
+
+// Workspace layout: [per-grid completion counters, n_cfgs x u32, padded to
+// 256 bytes | per-block partials, n_blocks x 4 doubles]. The counters sit at a
+// fixed place whatever the block count of a launch (which changes when grids
+// finish), so they stay zero between steps.
+static int64_t counters_bytes(int32_t n_cfgs) { return ((int64_t)n_cfgs * 4 + 255) / 256 * 256; }
+
+int batched_workspace_bytes(int32_t n_blocks, int32_t n_cfgs, int64_t *bytes) {
+    if (n_blocks < 1 || n_cfgs < 1) return set_error(PIC_E_INVALID, "n_blocks and n_cfgs must be >= 1");
+    *bytes = counters_bytes(n_cfgs) + (int64_t)n_blocks * 4 * 8;
+    return PIC_OK;
+}
+
+int batched_loop(const BatchLaunch &L, cudaStream_t st) {
+    constexpr int BLOCK = 256, WARPS = 8;
+    unsigned int *counters = reinterpret_cast<unsigned int *>(L.workspace);
+    double *partials = reinterpret_cast<double *>(reinterpret_cast<char *>(L.workspace) + counters_bytes(L.n_cfgs));
+    for (int64_t s = 0; s < L.n_steps; ++s) {
+        const int64_t step = L.first_step + s;
+        const int bi = (int)(step & 1), bo = bi ^ 1;
+        const int64_t t0 = L.step_task_off[s], t1 = L.step_task_off[s + 1];
+        const int64_t tracks = L.step_tracks[s];
+        if (tracks > 0 && t1 > t0) {
+            const unsigned blocks = (unsigned)((tracks + WARPS - 1) / WARPS);
+            if (L.dtype == PIC_F64)
+                batched_deposit_kernel<double, WARPS><<<blocks, WARPS * 32, 0, st>>>(
+                    L.cfgs, L.task_cfg + t0, L.task_first + t0, L.task_prefix + t0, (int)(t1 - t0), tracks, L.xs,
+                    L.ys, (double *)L.dens[bi], L.counts);
+            else
+                batched_deposit_kernel<float, WARPS><<<blocks, WARPS * 32, 0, st>>>(
+                    L.cfgs, L.task_cfg + t0, L.task_first + t0, L.task_prefix + t0, (int)(t1 - t0), tracks, L.xs,
+                    L.ys, (float *)L.dens[bi], L.counts);
+            int rc = check_launch("batched_deposit_kernel");
+            if (rc) return rc;
+        }
+        if (L.dtype == PIC_F64) {
+            BatchStepArgs<double> b{L.cfgs, L.blk_cfg, L.blk_item0, L.blk_item1, L.cfg_blk0, L.cfg_nblk,
+                                    (const double *)L.pos[bi], (const double *)L.neg[bi], (double *)L.pos[bo],
+                                    (double *)L.neg[bo], (const double *)L.dens[bi], (double *)L.dens[bo],
+                                    L.tally, partials, counters, step};
+            batched_step_kernel<double, BLOCK><<<(unsigned)L.n_blocks, BLOCK, 0, st>>>(b);
+        } else {
+            BatchStepArgs<float> b{L.cfgs, L.blk_cfg, L.blk_item0, L.blk_item1, L.cfg_blk0, L.cfg_nblk,
+                                   (const float *)L.pos[bi], (const float *)L.neg[bi], (float *)L.pos[bo],
+                                   (float *)L.neg[bo], (const float *)L.dens[bi], (float *)L.dens[bo],
+                                   L.tally, partials, counters, step};
+            batched_step_kernel<float, BLOCK><<<(unsigned)L.n_blocks, BLOCK, 0, st>>>(b);
+        }
+        int rc = check_launch("batched_step_kernel");
+        if (rc) return rc;
+    }
+    return PIC_OK;
+}
+
+}  // namespace pic

@@ -187,6 +187,29 @@ static int check_segment(const pic_grid *g, void *pos0, void *neg0, void *pos1, 
     return PIC_OK;
 }
 
+static int check_batch(const pic_batch_launch *L) {
+    if (!L) return set_error(PIC_E_INVALID, "launch descriptor is null");
+    if (L->dtype != PIC_F32 && L->dtype != PIC_F64) return set_error(PIC_E_INVALID, "dtype must be PIC_F32 or PIC_F64");
+    if (L->n_cfgs < 1 || L->n_blocks < 1) return set_error(PIC_E_INVALID, "n_cfgs and n_blocks must be >= 1");
+    if (L->n_steps < 0 || L->first_step < 0) return set_error(PIC_E_INVALID, "step range must be non-negative");
+    if (!L->cfgs || !L->blk_cfg || !L->blk_item0 || !L->blk_item1 || !L->cfg_blk0 || !L->cfg_nblk || !L->counts ||
+        !L->tally || !L->workspace || !L->dens[0] || !L->dens[1])
+        return set_error(PIC_E_INVALID, "null pointer in the batch launch descriptor");
+    int rc = check_fields(L->pos[0], L->neg[0], L->pos[1], L->neg[1]);
+    if (rc) return rc;
+    int64_t need = 0;
+    if ((rc = batched_workspace_bytes(L->n_blocks, L->n_cfgs, &need))) return rc;
+    if (L->workspace_bytes < need) return set_error(PIC_E_INVALID, "workspace too small (pic_batched_workspace_bytes)");
+    if (!L->step_task_off || !L->step_tracks) return set_error(PIC_E_INVALID, "step task tables are null");
+    for (int64_t s = 0; s < L->n_steps; ++s) {
+        if (L->step_task_off[s + 1] < L->step_task_off[s] || L->step_tracks[s] < 0)
+            return set_error(PIC_E_INVALID, "step task offsets must be non-decreasing");
+        if (L->step_tracks[s] > 0 && (!L->task_cfg || !L->task_first || !L->task_prefix || !L->xs || !L->ys))
+            return set_error(PIC_E_INVALID, "track or task arrays are null");
+    }
+    return PIC_OK;
+}
+
 }  // namespace pic
 
 using namespace pic;
@@ -324,6 +347,51 @@ int pic_graph_create(const pic_grid *g, void *pos0, void *neg0, void *pos1, void
     }
     rc = run_loop(g, pos0, neg0, pos1, neg1, parity, n_steps, xs, ys, track_offsets, dens0, dens1, dens_parity,
                   counts, tally, workspace, st);
+    e = cudaStreamEndCapture(st, &graph);
+    if (own) cudaStreamDestroy(own);
+    if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (e != cudaSuccess) return set_cuda_error("cudaStreamEndCapture", e);
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return set_cuda_error("cudaGraphInstantiate", e);
+    *graph_out = reinterpret_cast<uintptr_t>(exec);
+    return PIC_OK;
+}
+
+int pic_batched_workspace_bytes(int32_t n_blocks, int32_t n_cfgs, int64_t *bytes) {
+    if (!bytes) return set_error(PIC_E_INVALID, "bytes is null");
+    return batched_workspace_bytes(n_blocks, n_cfgs, bytes);
+}
+
+int pic_batched_segment(const pic_batch_launch *launch, uintptr_t stream) {
+    int rc = check_batch(launch);
+    if (rc) return rc;
+    return batched_loop(*launch, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int pic_batched_graph_create(const pic_batch_launch *launch, uintptr_t stream, uintptr_t *graph_out) {
+    if (!graph_out) return set_error(PIC_E_INVALID, "graph_out is null");
+    *graph_out = 0;
+    int rc = check_batch(launch);
+    if (rc) return rc;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    cudaStream_t own = nullptr;
+    if (st == nullptr) {
+        cudaError_t e = cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return set_cuda_error("cudaStreamCreateWithFlags", e);
+        st = own;
+    }
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        if (own) cudaStreamDestroy(own);
+        return set_cuda_error("cudaStreamBeginCapture", e);
+    }
+    rc = batched_loop(*launch, st);
     e = cudaStreamEndCapture(st, &graph);
     if (own) cudaStreamDestroy(own);
     if (rc) {

@@ -86,6 +86,10 @@ int launch_step(const pic_grid *g, const void *pos_in, const void *neg_in, void 
                 const void *dens, void *dens_zero, double *tally, void *ws, cudaStream_t st);
 int launch_deposit(const pic_grid *g, const double *xs, const double *ys, int64_t m, void *dens,
                    uint32_t *counts, cudaStream_t st);
+using BatchLaunch = pic_batch_launch;
+int batched_workspace_bytes(int32_t n_blocks, int32_t n_cfgs, int64_t *bytes);
+int batched_loop(const BatchLaunch &L, cudaStream_t st);
+
 int step_noalloc(const pic_grid *g, const void *pos_in, const void *neg_in, void *pos_out, void *neg_out,
                  const double *xs, const double *ys, int64_t n_tracks, uint32_t *counts, double *tally,
                  cudaStream_t st);

@@ -1,0 +1,88 @@
+"""Batched runs: many configurations advanced together give each
+configuration's own result (same tracks, same tallies to float32 rounding),
+and the saturation-sweep definition is the documented one."""
+
+import numpy as np
+import pytest
+
+from goldens import make_config, pkg
+
+KS_ABS = 1e-5
+
+
+def _mixed_batch(dtype_note=""):
+    return [
+        make_config("fast"),
+        make_config("fast_dense", lateral_boundary="reflecting"),
+        make_config("small_run"),
+        make_config("rf_odd_noxy", scoring_region="full_grid"),
+        make_config("fast_two_species"),
+        make_config("aic144_dev"),
+    ]
+
+
+def test_saturation_sweep_definition():
+    cfgs = pkg().saturation_sweep_configs()
+    assert len(cfgs) == 64
+    volts = [c.voltage_V for c in cfgs]
+    assert volts[0] == pytest.approx(25.0) and volts[-1] == pytest.approx(400.0)
+    assert all(b > a for a, b in zip(volts, volts[1:]))
+    assert {c.electrode_gap_cm for c in cfgs} <= {0.1, 0.2, 0.3}
+    assert all(1.0 <= c.dose_rate_Gy_s <= 100.0 for c in cfgs)
+    assert all(100e-6 <= c.pulse_duration_s <= 1000e-6 for c in cfgs)
+    assert {c.grid_size_um for c in cfgs} <= {5.0, 10.0}
+    assert all(0.008 <= c.sampled_radius_cm <= 0.03 for c in cfgs)
+    assert [c.seed for c in cfgs] == list(range(1, 65))
+    sizes = [c.no_xy ** 2 * c.no_z_with_buffer for c in cfgs]
+    assert max(sizes) / min(sizes) > 10  # uneven voxel counts
+    again = pkg().saturation_sweep_configs()
+    assert [c.number_of_tracks_per_pulse for c in again] == [c.number_of_tracks_per_pulse for c in cfgs]
+
+
+def test_phases_cover_every_step_once():
+    import importlib
+
+    b = importlib.import_module(pkg().__name__ + ".batched")
+    ph = b._phases([5, 3, 5, 9])
+    assert ph == [(0, 3, [0, 1, 2, 3]), (3, 5, [0, 2, 3]), (5, 9, [3])]
+
+
+@pytest.mark.gpu
+def test_batched_matches_individual_runs():
+    cfgs = _mixed_batch()
+    batch = pkg().run_batched_b200(cfgs, return_fields=True)
+    for cfg, got in zip(cfgs, batch):
+        ref = pkg().run_simulation_b200(cfg, progress=False, use_graphs=False, shape={"variant": "flat"})
+        np.testing.assert_array_equal(got.track_density_xy, ref.track_density_xy)
+        assert abs(got.ks - ref.ks) <= 1e-6
+        for x, y in [(got.recombination, ref.recombination), (got.injected_positive, ref.injected_positive),
+                     (got.n_positive, ref.n_positive), (got.n_negative, ref.n_negative)]:
+            np.testing.assert_allclose(x, y, rtol=0, atol=1e-6 * max(np.abs(y).max(), 1e-300))
+        peak = np.abs(ref.positive_array).max()
+        np.testing.assert_allclose(got.positive_array, ref.positive_array, rtol=0, atol=peak * 1e-6)
+        np.testing.assert_allclose(got.negative_array, ref.negative_array, rtol=0, atol=peak * 1e-6)
+
+
+@pytest.mark.gpu
+def test_batched_float64_matches_the_oracle(oracle):
+    cfgs = _mixed_batch()
+    batch = pkg().run_batched_b200(cfgs, dtype="float64")
+    for cfg, got in zip(cfgs, batch):
+        ref = oracle.run(cfg, mode="batched", threads=2, keep_fields=False)
+        np.testing.assert_array_equal(got.track_density_xy, ref["track_density_xy"])
+        assert got.ks == pytest.approx(ref["ks"], rel=1e-9)
+        np.testing.assert_allclose(got.recombination, ref["recombined"], rtol=1e-9,
+                                   atol=1e-9 * np.abs(ref["recombined"]).max())
+
+
+@pytest.mark.gpu
+def test_batched_sweep_subset_matches_the_oracle(oracle):
+    """Eight configurations of the saturation sweep (uneven sizes and step
+    counts), float32 batch against the float64 oracle at |dk_s| <= 1e-5."""
+    cfgs = [c for c in pkg().saturation_sweep_configs() if c.no_xy ** 2 * c.no_z_with_buffer < 1.5e6][:8]
+    assert len(cfgs) == 8
+    batch = pkg().run_batched_b200(cfgs)
+    for cfg, got in zip(cfgs, batch):
+        ref = oracle.run(cfg, mode="batched", threads=8, keep_fields=False)
+        np.testing.assert_array_equal(got.track_density_xy, ref["track_density_xy"])
+        assert abs(got.ks - ref["ks"]) <= KS_ABS
