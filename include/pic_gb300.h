@@ -72,7 +72,9 @@ typedef struct pic_grid {
 /* Fused-step kernels. FLAT: one thread per four k of a column, neighbours
  * through L1/L2, any grid and either field type. STREAM: float32 only; whole
  * (j-tile x k-row) planes staged in shared memory by bulk asynchronous copies
- * while the CTA marches along i, for grids with no_xy >= 16. AUTO picks. */
+ * while the CTA marches along i, for grids with no_xy >= 16. AUTO picks
+ * STREAM for float32 grids with no_xy >= 64 and no_xy^2 * kpitch >= 6e6 cells,
+ * FLAT otherwise; planes_per_item 0 gives about 12 work items per SM. */
 #define PIC_VARIANT_AUTO 0
 #define PIC_VARIANT_FLAT 1
 #define PIC_VARIANT_STREAM 2
@@ -172,6 +174,35 @@ int pic_step_noalloc(const pic_grid *g, const void *pos_in, const void *neg_in, 
                      uintptr_t stream);
 
 /*
+ * pic_sample_disc -- the rejection step of the host track sampler (no GPU).
+ * Replaces the block loop of CylinderSampler.sample
+ * (pulsed_ion_chamber/pulses.py:84-171; per track :64-82): pair a of the
+ * caller's uniforms u[0 .. 2*n_pairs) gives x = u[2a] * scale,
+ * y = u[2a+1] * scale, accepted when (x-mid)^2 + (y-mid)^2 <= radius_sq, in
+ * float64 with one rounding per operation (bit-identical to the reference's
+ * NumPy expression). Scans pairs in order until n_wanted centres are accepted
+ * or the pairs run out; writes the centres to xs/ys and sets *n_accepted and
+ * *n_pairs_used (pairs consumed, including the last accepted one).
+ */
+int pic_sample_disc(const double *u, int64_t n_pairs, double scale, double mid, double radius_sq, int64_t n_wanted,
+                    double *xs, double *ys, int64_t *n_accepted, int64_t *n_pairs_used);
+
+/*
+ * pic_sample_disc_pcg64 -- the same scan, drawing the uniforms itself from a
+ * NumPy PCG64 generator's state (the reference seeds np.random.default_rng,
+ * a PCG64): state[4] = {state_hi, state_lo, inc_hi, inc_lo} as in
+ * bit_generator.state. Each uniform is one PCG64 XSL-RR 128/64 output
+ * converted as NumPy's random() does ((out >> 11) * 2^-53), so the centres are
+ * bit-identical to drawing with the generator and scanning as above. Stops at
+ * n_wanted accepted centres or after max_pairs pairs; advances state[0..1]
+ * past exactly the *n_draws uniforms it consumed (the caller writes the state
+ * back to its generator). No counterpart in the reference as a function: it
+ * fuses the reference's draw (pulses.py:84-171) and scan.
+ */
+int pic_sample_disc_pcg64(uint64_t *state, double scale, double mid, double radius_sq, int64_t n_wanted,
+                          int64_t max_pairs, double *xs, double *ys, int64_t *n_accepted, int64_t *n_draws);
+
+/*
  * pic_run_segment -- n_steps consecutive time steps on the device.
  *
  * Step s (0-based within the segment) reads fields[(parity + s) & 1] and
@@ -235,7 +266,9 @@ typedef struct pic_batch_launch {
     const int32_t *blk_cfg;                /* device, per block: its grid                    */
     const int64_t *blk_item0, *blk_item1;  /* device, per block: its item range              */
     int32_t n_blocks;
-    int32_t reserved;
+    int32_t index32;                       /* 1: every grid has no_xy <= 16383 and          */
+                                           /*  no_xy^2 * kpitch < 2^31 (32-bit offsets, the  */
+                                           /*  faster decode); 0: 64-bit offsets (any grid)  */
     const int32_t *cfg_blk0, *cfg_nblk;    /* device, per grid: first block, block count     */
     void *pos[2], *neg[2];                 /* device, packed fields of time levels 0 and 1   */
     void *dens[2];                         /* device, packed densities, by step parity       */

@@ -52,7 +52,7 @@ class PicBatchLaunch(ctypes.Structure):
         ("blk_item0", ctypes.c_void_p),
         ("blk_item1", ctypes.c_void_p),
         ("n_blocks", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("index32", ctypes.c_int32),
         ("cfg_blk0", ctypes.c_void_p),
         ("cfg_nblk", ctypes.c_void_p),
         ("pos", ctypes.c_void_p * 2),
@@ -247,6 +247,8 @@ def run_batched_b200(
             cfg_nblk=torch.from_numpy(cfg_nblk).to(dev),
             n_blocks=len(blk_cfg),
         )))
+    # 32-bit offsets when every grid's fields are < 2^31 elements
+    index32 = all(int(g.no_xy) <= 16383 and int(g.no_xy) ** 2 * int(g.kpitch) < 2**31 for g in grids)
     wsb = ctypes.c_int64()
     N.check(lib.pic_batched_workspace_bytes(max_blocks, n_cfg, ctypes.byref(wsb)), "pic_batched_workspace_bytes")
     workspace = torch.zeros(int(wsb.value), dtype=torch.uint8, device=dev)
@@ -265,6 +267,7 @@ def run_batched_b200(
             L.blk_item0 = tab["blk_item0"].data_ptr()
             L.blk_item1 = tab["blk_item1"].data_ptr()
             L.n_blocks = tab["n_blocks"]
+            L.index32 = int(index32)
             L.cfg_blk0 = tab["cfg_blk0"].data_ptr()
             L.cfg_nblk = tab["cfg_nblk"].data_ptr()
             L.pos[0], L.pos[1] = pos[0].data_ptr(), pos[1].data_ptr()

@@ -25,7 +25,7 @@ BUILD = PKG / "_build"
 LIB = BUILD / "libpic_gb300.so"
 INCLUDE = PKG.parent / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC,-O3",
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC,-O3,-ffp-contract=off",
               "-Xptxas", "-O3"]
 
 

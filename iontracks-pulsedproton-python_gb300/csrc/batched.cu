@@ -70,9 +70,29 @@ __device__ void grid_args(const pic_batch_cfg &C, const BatchStepArgs<T> &b, Ste
     a.injected_scale = g.gaussian_factor * (double)g.no_z;
 }
 
-template <typename T, int BLOCK>
+// Reduction type of a grid's tallies: double-float for float32 fields (no
+// float64 arithmetic), float64 for float64 fields; partial slots are 8 bytes
+// either way.
+template <typename T> struct RedT { using type = double; };
+template <> struct RedT<float> { using type = DF; };
+__device__ __forceinline__ double red_value(double v) { return v; }
+__device__ __forceinline__ double red_value(DF v) { return df_value(v); }
+__device__ __forceinline__ void red_store(double *slot, double v) { *slot = v; }
+__device__ __forceinline__ void red_store(double *slot, DF v) {
+    *reinterpret_cast<float2 *>(slot) = make_float2(v.hi, v.lo);
+}
+__device__ __forceinline__ void red_load_add(double &acc, const double *slot) { acc += __ldcg(slot); }
+__device__ __forceinline__ void red_load_add(DF &acc, const double *slot) {
+    const float2 p = __ldcg(reinterpret_cast<const float2 *>(slot));
+    acc = df_add(acc, DF{p.x, p.y});
+}
+__device__ __forceinline__ double red_of(const Tally<double> &t) { return t.value(); }
+__device__ __forceinline__ DF red_of(const Tally<float> &t) { return df_of(t); }
+
+template <typename T, int BLOCK, typename I>
 __global__ void __launch_bounds__(BLOCK) batched_step_kernel(BatchStepArgs<T> b) {
-    __shared__ double red[BLOCK / 32][4];
+    using R = typename RedT<T>::type;
+    __shared__ R red[BLOCK / 32][4];
     __shared__ bool last;
     // the block's grid arguments, staged once in shared memory and read by
     // broadcast (keeps them out of the registers of every thread)
@@ -83,14 +103,14 @@ __global__ void __launch_bounds__(BLOCK) batched_step_kernel(BatchStepArgs<T> b)
     if (threadIdx.x == 0) grid_args(C, b, a);
     __syncthreads();
     Tally<T> t_rec, t_p, t_n, t_inj;
-    const int64_t i1 = b.blk_item1[blk];
-    for (int64_t item = b.blk_item0[blk] + threadIdx.x; item < i1; item += BLOCK)
-        flat_item(a, item, t_rec, t_p, t_n, t_inj);
-    double v[4] = {t_inj.value(), t_rec.value(), t_p.value(), t_n.value()};
+    const I i1 = (I)b.blk_item1[blk];
+    for (I item = (I)b.blk_item0[blk] + threadIdx.x; item < i1; item += BLOCK)
+        flat_item<T, I>(a, item, t_rec, t_p, t_n, t_inj);
+    R v[4] = {red_of(t_inj), red_of(t_rec), red_of(t_p), red_of(t_n)};
     block_sum4<BLOCK>(v, red);
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q) b.partials[4 * (int64_t)blk + q] = v[q];
+        for (int q = 0; q < 4; ++q) red_store(b.partials + 4 * (int64_t)blk + q, v[q]);
         __threadfence();
         last = (atomicAdd(b.counters + c, 1u) == (unsigned)b.cfg_nblk[c] - 1u);
     }
@@ -98,17 +118,17 @@ __global__ void __launch_bounds__(BLOCK) batched_step_kernel(BatchStepArgs<T> b)
     if (!last) return;
     __threadfence();
     const int b0 = b.cfg_blk0[c], nb = b.cfg_nblk[c];
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    R acc[4] = {R{}, R{}, R{}, R{}};
     for (int k = threadIdx.x; k < nb; k += BLOCK)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) acc[q] += __ldcg(b.partials + 4 * (int64_t)(b0 + k) + q);
+        for (int q = 0; q < 4; ++q) red_load_add(acc[q], b.partials + 4 * (int64_t)(b0 + k) + q);
     block_sum4<BLOCK>(acc, red);
     if (threadIdx.x == 0) {
         double *t = b.tally + 4 * (C.tally_off + b.step);
-        t[0] = acc[0] * a.injected_scale;
-        t[1] = acc[1];
-        t[2] = acc[2];
-        t[3] = acc[3];
+        t[0] = red_value(acc[0]) * a.injected_scale;
+        t[1] = red_value(acc[1]);
+        t[2] = red_value(acc[2]);
+        t[3] = red_value(acc[3]);
         b.counters[c] = 0u;
         __threadfence();
     }
@@ -148,8 +168,18 @@ int batched_workspace_bytes(int32_t n_blocks, int32_t n_cfgs, int64_t *bytes) {
     return PIC_OK;
 }
 
+template <typename T, typename I>
+static void launch_batched_step(const BatchLaunch &L, int bi, int bo, double *partials, unsigned int *counters,
+                                int64_t step, cudaStream_t st) {
+    constexpr int BLOCK = 256;
+    BatchStepArgs<T> b{L.cfgs, L.blk_cfg, L.blk_item0, L.blk_item1, L.cfg_blk0, L.cfg_nblk,
+                       (const T *)L.pos[bi], (const T *)L.neg[bi], (T *)L.pos[bo], (T *)L.neg[bo],
+                       (const T *)L.dens[bi], (T *)L.dens[bo], L.tally, partials, counters, step};
+    batched_step_kernel<T, BLOCK, I><<<(unsigned)L.n_blocks, BLOCK, 0, st>>>(b);
+}
+
 int batched_loop(const BatchLaunch &L, cudaStream_t st) {
-    constexpr int BLOCK = 256, WARPS = 8;
+    constexpr int WARPS = 8;
     unsigned int *counters = reinterpret_cast<unsigned int *>(L.workspace);
     double *partials = reinterpret_cast<double *>(reinterpret_cast<char *>(L.workspace) + counters_bytes(L.n_cfgs));
     for (int64_t s = 0; s < L.n_steps; ++s) {
@@ -171,17 +201,11 @@ int batched_loop(const BatchLaunch &L, cudaStream_t st) {
             if (rc) return rc;
         }
         if (L.dtype == PIC_F64) {
-            BatchStepArgs<double> b{L.cfgs, L.blk_cfg, L.blk_item0, L.blk_item1, L.cfg_blk0, L.cfg_nblk,
-                                    (const double *)L.pos[bi], (const double *)L.neg[bi], (double *)L.pos[bo],
-                                    (double *)L.neg[bo], (const double *)L.dens[bi], (double *)L.dens[bo],
-                                    L.tally, partials, counters, step};
-            batched_step_kernel<double, BLOCK><<<(unsigned)L.n_blocks, BLOCK, 0, st>>>(b);
+            if (L.index32) launch_batched_step<double, uint32_t>(L, bi, bo, partials, counters, step, st);
+            else launch_batched_step<double, int64_t>(L, bi, bo, partials, counters, step, st);
         } else {
-            BatchStepArgs<float> b{L.cfgs, L.blk_cfg, L.blk_item0, L.blk_item1, L.cfg_blk0, L.cfg_nblk,
-                                   (const float *)L.pos[bi], (const float *)L.neg[bi], (float *)L.pos[bo],
-                                   (float *)L.neg[bo], (const float *)L.dens[bi], (float *)L.dens[bo],
-                                   L.tally, partials, counters, step};
-            batched_step_kernel<float, BLOCK><<<(unsigned)L.n_blocks, BLOCK, 0, st>>>(b);
+            if (L.index32) launch_batched_step<float, uint32_t>(L, bi, bo, partials, counters, step, st);
+            else launch_batched_step<float, int64_t>(L, bi, bo, partials, counters, step, st);
         }
         int rc = check_launch("batched_step_kernel");
         if (rc) return rc;

@@ -77,8 +77,14 @@ int score_test(const pic_grid *g, ScoreTest *out) {
 }
 
 int resolve_shape(pic_grid *g) {
+    // Measured on GB300: below ~6 M cells a step is latency-bound and the flat
+    // kernel is as fast as the best streaming shape (or faster); above, the
+    // streaming kernel wins (0.088 vs 0.102 ms at 208x208x408, 0.51 vs 0.74 ms
+    // at 608x608x408).
     if (g->variant == PIC_VARIANT_AUTO)
-        g->variant = (g->dtype == PIC_F32 && g->no_xy >= 64) ? PIC_VARIANT_STREAM : PIC_VARIANT_FLAT;
+        g->variant = (g->dtype == PIC_F32 && g->no_xy >= 64 && g->no_xy * g->no_xy * g->kpitch >= kStreamMinCells)
+                         ? PIC_VARIANT_STREAM
+                         : PIC_VARIANT_FLAT;
     if (g->variant == PIC_VARIANT_FLAT) return PIC_OK;
     if (g->variant != PIC_VARIANT_STREAM) return set_error(PIC_E_INVALID, "variant must be PIC_VARIANT_AUTO, _FLAT or _STREAM");
     if (g->dtype != PIC_F32) return set_error(PIC_E_INVALID, "the stream variant supports float32 fields only");
@@ -116,7 +122,14 @@ int resolve_shape(pic_grid *g) {
     if (g->stages > 16) return set_error(PIC_E_INVALID, "stream variant: at most 16 stages");
     if (stream_smem_bytes(g->tile_rows, kp, g->stages) > budget)
         return set_error(PIC_E_CAPACITY, "stream variant: tile_rows x stages exceed shared memory");
-    if (g->planes_per_item <= 0) g->planes_per_item = 64;
+    if (g->planes_per_item <= 0) {
+        // about 12 work items per SM (a whole item per CTA keeps the load
+        // balanced and the ring full), between 4 and 64 planes per item
+        const int64_t jt = (g->no_xy - 2 + g->tile_rows - 1) / g->tile_rows;
+        const int64_t target = 12LL * sm_count();
+        int64_t li = ((g->no_xy - 2) * jt + target - 1) / target;
+        g->planes_per_item = (int32_t)(li < 4 ? 4 : (li > 64 ? 64 : li));
+    }
     if (g->ctas_per_sm <= 0) g->ctas_per_sm = 1;
     return PIC_OK;
 }
@@ -192,6 +205,7 @@ static int check_batch(const pic_batch_launch *L) {
     if (L->dtype != PIC_F32 && L->dtype != PIC_F64) return set_error(PIC_E_INVALID, "dtype must be PIC_F32 or PIC_F64");
     if (L->n_cfgs < 1 || L->n_blocks < 1) return set_error(PIC_E_INVALID, "n_cfgs and n_blocks must be >= 1");
     if (L->n_steps < 0 || L->first_step < 0) return set_error(PIC_E_INVALID, "step range must be non-negative");
+    if (L->index32 != 0 && L->index32 != 1) return set_error(PIC_E_INVALID, "index32 must be 0 or 1");
     if (!L->cfgs || !L->blk_cfg || !L->blk_item0 || !L->blk_item1 || !L->cfg_blk0 || !L->cfg_nblk || !L->counts ||
         !L->tally || !L->workspace || !L->dens[0] || !L->dens[1])
         return set_error(PIC_E_INVALID, "null pointer in the batch launch descriptor");
@@ -310,6 +324,23 @@ int pic_step_noalloc(const pic_grid *g, const void *pos_in, const void *neg_in, 
     if (n_tracks > 0 && (!xs || !ys)) return set_error(PIC_E_INVALID, "track arrays are null");
     return step_noalloc(g, pos_in, neg_in, pos_out, neg_out, xs, ys, n_tracks, counts, tally,
                         reinterpret_cast<cudaStream_t>(stream));
+}
+
+int pic_sample_disc(const double *u, int64_t n_pairs, double scale, double mid, double radius_sq, int64_t n_wanted,
+                    double *xs, double *ys, int64_t *n_accepted, int64_t *n_pairs_used) {
+    if (n_pairs < 0 || n_wanted < 0) return set_error(PIC_E_INVALID, "n_pairs and n_wanted must be >= 0");
+    if (!n_accepted || !n_pairs_used) return set_error(PIC_E_INVALID, "null pointer argument");
+    if ((n_pairs > 0 && !u) || (n_wanted > 0 && (!xs || !ys))) return set_error(PIC_E_INVALID, "null pointer argument");
+    return sample_disc(u, n_pairs, scale, mid, radius_sq, n_wanted, xs, ys, n_accepted, n_pairs_used);
+}
+
+int pic_sample_disc_pcg64(uint64_t *state, double scale, double mid, double radius_sq, int64_t n_wanted,
+                          int64_t max_pairs, double *xs, double *ys, int64_t *n_accepted, int64_t *n_draws) {
+    if (!state || !n_accepted || !n_draws) return set_error(PIC_E_INVALID, "null pointer argument");
+    if (n_wanted < 0 || max_pairs < 0) return set_error(PIC_E_INVALID, "n_wanted and max_pairs must be >= 0");
+    if (n_wanted > 0 && (!xs || !ys)) return set_error(PIC_E_INVALID, "null pointer argument");
+    if ((state[3] & 1u) == 0u) return set_error(PIC_E_INVALID, "a PCG64 increment is odd");
+    return sample_disc_pcg64(state, scale, mid, radius_sq, n_wanted, max_pairs, xs, ys, n_accepted, n_draws);
 }
 
 int pic_run_segment(const pic_grid *g, void *pos0, void *neg0, void *pos1, void *neg1, int64_t parity,

@@ -11,8 +11,9 @@
 // solver_numba.py:86-89.
 //
 // The density is laid out [no_xy][dens_pitch(no_xy)] (rows padded to 16
-// bytes). One warp per track. Lanes own stencil columns j; row factors are computed
-// 32 rows at a time, one row per lane, and broadcast by shuffle. Each cell is
+// bytes). One to eight warps per track (more when the step has few tracks),
+// splitting the box's rows. Lanes own stencil columns j; row factors are
+// computed 32 rows at a time, one row per lane, and broadcast by shuffle. Each cell is
 // added with a float atomic: tracks overlap, and the L2 resolves the
 // collisions. The offset (i - x) is formed in float64 from the float64 track
 // centre before it is rounded, so the Gaussian is not shifted by the float32
@@ -27,28 +28,42 @@
 
 namespace pic {
 
+// `parts` warps per track (a power of two dividing WARPS).
 template <typename T, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) deposit_kernel(const double *__restrict__ xs,
                                                               const double *__restrict__ ys, int64_t m,
                                                               T *__restrict__ dens, uint32_t *__restrict__ counts,
-                                                              int64_t n, int64_t dp, double cut, T h2b2) {
-    const int64_t t = (int64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
+                                                              int64_t n, int64_t dp, double cut, T h2b2, int parts) {
+    const int warp = threadIdx.x >> 5;
+    const int64_t t = (int64_t)blockIdx.x * (WARPS / parts) + warp / parts;
     if (t >= m) return;
-    deposit_track<T>(xs[t], ys[t], n, dp, cut, h2b2, dens, counts, threadIdx.x & 31);
+    deposit_track<T>(xs[t], ys[t], n, dp, cut, h2b2, dens, counts, threadIdx.x & 31, warp % parts, parts);
+}
+
+// Warps per track: a step's tracks alone rarely fill the GPU (a few to a few
+// thousand per step), so with few tracks each box is shared by up to 8 warps.
+static int deposit_parts(int64_t m, int sms) {
+    const int64_t warps = (int64_t)sms * 32;  // half the resident warps of the GPU
+    int p = 8;
+    while (p > 1 && m * p > warps) p >>= 1;
+    return p;
 }
 
 int launch_deposit(const pic_grid *g, const double *xs, const double *ys, int64_t m, void *dens, uint32_t *counts,
                    cudaStream_t st) {
     if (m <= 0) return PIC_OK;
     constexpr int WARPS = 8;
-    const int64_t blocks = (m + WARPS - 1) / WARPS;
+    const int parts = deposit_parts(m, sm_count());
+    const int per_block = WARPS / parts;
+    const int64_t blocks = (m + per_block - 1) / per_block;
     if (g->dtype == PIC_F64) {
         deposit_kernel<double, WARPS><<<(unsigned)blocks, WARPS * 32, 0, st>>>(
-            xs, ys, m, (double *)dens, counts, g->no_xy, dens_pitch(g->no_xy), g->cutoff_voxels, g->h2_over_b2);
+            xs, ys, m, (double *)dens, counts, g->no_xy, dens_pitch(g->no_xy), g->cutoff_voxels, g->h2_over_b2,
+            parts);
     } else {
         deposit_kernel<float, WARPS><<<(unsigned)blocks, WARPS * 32, 0, st>>>(
             xs, ys, m, (float *)dens, counts, g->no_xy, dens_pitch(g->no_xy), g->cutoff_voxels,
-            (float)g->h2_over_b2);
+            (float)g->h2_over_b2, parts);
     }
     return check_launch("deposit_kernel");
 }

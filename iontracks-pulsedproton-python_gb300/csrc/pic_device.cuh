@@ -53,6 +53,32 @@ struct Tally {
     }
     __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
+
+// Double-float: the unevaluated sum hi + lo of two floats, added with the
+// error-free TwoSum of Knuth (TAOCP vol. 2, 4.2.2) and renormalised with
+// Dekker's FastTwoSum (1971) -- about 44 significant bits from FP32
+// instructions only. The block and grid reductions of the float32 kernels use
+// it in place of float64, whose rate on GB300 is a small fraction of FP32's
+// (a float64 reduction tree was several microseconds of every small-grid step).
+// Additions only: nothing here can be contracted into an FMA.
+struct DF {
+    float hi, lo;
+};
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+    const float s = a.hi + b.hi;
+    const float v = s - a.hi;
+    const float e = (a.hi - (s - v)) + (b.hi - v);
+    const float lo = e + (a.lo + b.lo);
+    const float h = s + lo;
+    return {h, lo - (h - s)};
+}
+// A Kahan running sum (s, c) holds s - c.
+__device__ __forceinline__ DF df_of(const Tally<float> &t) {
+    const float h = t.s - t.c;
+    return {h, (t.s - h) - t.c};
+}
+__device__ __forceinline__ double df_value(DF a) { return (double)a.hi + (double)a.lo; }
+
 template <>
 struct Tally<double> {
     double s = 0;
@@ -66,9 +92,19 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// Block-wide sum of four doubles, result valid in thread 0. Fixed tree order.
-template <int BLOCK>
-__device__ __forceinline__ void block_sum4(double (&v)[4], double (*smem)[4]) {
+__device__ __forceinline__ DF warp_sum(DF a) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const DF b{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
+        a = df_add(a, b);
+    }
+    return a;
+}
+
+// Block-wide sum of four doubles (or double-floats), result valid in thread
+// 0. Fixed tree order.
+template <int BLOCK, typename A>
+__device__ __forceinline__ void block_sum4(A (&v)[4], A (*smem)[4]) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int q = 0; q < 4; ++q) v[q] = warp_sum(v[q]);
@@ -80,11 +116,49 @@ __device__ __forceinline__ void block_sum4(double (&v)[4], double (*smem)[4]) {
     if (warp == 0) {
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            double x = lane < BLOCK / 32 ? smem[lane][q] : 0.0;
+            A x = lane < BLOCK / 32 ? smem[lane][q] : A{};
             v[q] = warp_sum(x);
         }
     }
     __syncthreads();
+}
+
+// The double-float form of finish_tally (below) for float32 kernels: the
+// partials are float2 (hi, lo) pairs in the same 8-byte slots.
+template <int BLOCK>
+__device__ void finish_tally_df(DF (&v)[4], double *partials_d, unsigned int *counter, double *tally,
+                                double injected_scale) {
+    __shared__ DF red[BLOCK / 32][4];
+    __shared__ bool last;
+    float2 *partials = reinterpret_cast<float2 *>(partials_d);
+    block_sum4<BLOCK>(v, red);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) partials[4 * (int64_t)blockIdx.x + q] = make_float2(v[q].hi, v[q].lo);
+        __threadfence();
+        unsigned int prev = atomicAdd(counter, 1u);
+        last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    DF acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += BLOCK) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float2 p = __ldcg(partials + 4 * (int64_t)b + q);
+            acc[q] = df_add(acc[q], DF{p.x, p.y});
+        }
+    }
+    block_sum4<BLOCK>(acc, red);
+    if (threadIdx.x == 0) {
+        tally[0] = df_value(acc[0]) * injected_scale;
+        tally[1] = df_value(acc[1]);
+        tally[2] = df_value(acc[2]);
+        tally[3] = df_value(acc[3]);
+        *counter = 0u;  // ready for the next step
+        __threadfence();
+    }
 }
 
 // Completes a step's tallies: every block stores its partial, the last block

@@ -33,18 +33,37 @@ __device__ __forceinline__ T dep_at(const StepArgs<T> &a, int64_t dcol) {
     return a.dens ? a.gfac * a.dens[dcol] : T(0);
 }
 
+// Index type of a grid: 32-bit unsigned offsets when every element offset of
+// the fields fits (no_xy^2 * kpitch < 2^31) and the scored test fits 32-bit
+// arithmetic (no_xy <= 16383) -- every grid up to ~2 G cells; the item
+// decode then costs two 32-bit divisions instead of two 64-bit ones.
+inline bool flat_index32(int64_t n, int64_t kp) { return n <= 16383 && n * n * kp < ((int64_t)1 << 31); }
+
+template <typename I>
+__device__ __forceinline__ bool scored_col_t(const ScoreTest &t, I i, I j) {
+    if constexpr (sizeof(I) == 4) {
+        // |2i - two_mid| < 2^15 for no_xy <= 16383: the squares fit uint32
+        const int dx = 2 * (int)i - (int)t.two_mid, dy = 2 * (int)j - (int)t.two_mid;
+        const uint32_t r2 = (uint32_t)(dx * dx) + (uint32_t)(dy * dy);
+        return t.thr4 >= 0 && (t.thr4 >= 0xffffffffLL || r2 <= (uint32_t)t.thr4);
+    } else {
+        return scored_column(t, (int64_t)i, (int64_t)j);
+    }
+}
+
 // The fused step for one work item: four consecutive k of output column
 // (i, j), decoded from the flat item index (k-vector fastest). Adds the
-// item's scored contributions to the thread's running tallies.
-template <typename T>
-__device__ __forceinline__ void flat_item(const StepArgs<T> &a, int64_t item, Tally<T> &t_rec,
+// item's scored contributions to the thread's running tallies. I is the index
+// type (uint32_t when flat_index32 holds for the grid, else int64_t).
+template <typename T, typename I>
+__device__ __forceinline__ void flat_item(const StepArgs<T> &a, I item, Tally<T> &t_rec,
                                           Tally<T> &t_p, Tally<T> &t_n, Tally<T> &t_inj) {
-    const int64_t n = a.n, kp = a.kp;
-    const int64_t col = item / a.c4;
-    const int c = (int)(item - col * a.c4);
-    const int64_t i = col / n, j = col - i * n;
+    const I n = (I)a.n, kp = (I)a.kp, c4 = (I)a.c4, dp = (I)a.dp;
+    const I col = item / c4;
+    const int c = (int)(item - col * c4);
+    const I i = col / n, j = col - i * n;
     const int k0 = 4 * c;
-    if (c == 0 && a.dens_zero) a.dens_zero[i * a.dp + j] = T(0);
+    if (c == 0 && a.dens_zero) a.dens_zero[i * dp + j] = T(0);
 
     // gap mask of the four outputs and of the two z-neighbours
     bool g[4];
@@ -53,13 +72,13 @@ __device__ __forceinline__ void flat_item(const StepArgs<T> &a, int64_t item, Ta
     const bool g_km = (k0 - 1 >= a.nze) && (k0 - 1 < a.gap_end);
     const bool g_kp = (k0 + 4 >= a.nze) && (k0 + 4 < a.gap_end);
 
-    const int64_t ci = i < 1 ? 1 : (i > n - 2 ? n - 2 : i);
-    const int64_t cj = j < 1 ? 1 : (j > n - 2 ? n - 2 : j);
+    const I ci = i < 1 ? 1 : (i > n - 2 ? n - 2 : i);
+    const I cj = j < 1 ? 1 : (j > n - 2 ? n - 2 : j);
     const bool ring = (ci != i) || (cj != j);
-    const int64_t out_off = col * kp + k0;
+    const I out_off = col * kp + k0;
 
     if (ring && !a.reflecting) {
-        const T d = dep_at(a, i * a.dp + j);
+        const T d = dep_at(a, (int64_t)(i * dp + j));
         V4<T> P = load4(a.pos_in + out_off), N = load4(a.neg_in + out_off);
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
@@ -71,9 +90,9 @@ __device__ __forceinline__ void flat_item(const StepArgs<T> &a, int64_t item, Ta
         return;
     }
 
-    const int64_t ccol = ci * n + cj;
-    const int64_t base = ccol * kp + k0;
-    const int64_t di = n * kp;
+    const I ccol = ci * n + cj;
+    const I base = ccol * kp + k0;
+    const I di = n * kp;
     V4<T> P = load4(a.pos_in + base), N = load4(a.neg_in + base);
     V4<T> Pim = load4(a.pos_in + base - di), Pip = load4(a.pos_in + base + di);
     V4<T> Pjm = load4(a.pos_in + base - kp), Pjp = load4(a.pos_in + base + kp);
@@ -84,10 +103,10 @@ __device__ __forceinline__ void flat_item(const StepArgs<T> &a, int64_t item, Ta
     T pkp = k0 + 4 < kp ? a.pos_in[base + 4] : T(0);
     T nkp = k0 + 4 < kp ? a.neg_in[base + 4] : T(0);
 
-    const int64_t dcol = ci * a.dp + cj;
+    const I dcol = ci * dp + cj;
     if (a.dens) {
         const T dc = a.gfac * a.dens[dcol];
-        const T dim = a.gfac * a.dens[dcol - a.dp], dip = a.gfac * a.dens[dcol + a.dp];
+        const T dim = a.gfac * a.dens[dcol - dp], dip = a.gfac * a.dens[dcol + dp];
         const T djm = a.gfac * a.dens[dcol - 1], djp = a.gfac * a.dens[dcol + 1];
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
@@ -103,7 +122,7 @@ __device__ __forceinline__ void flat_item(const StepArgs<T> &a, int64_t item, Ta
         if (g_kp) { pkp += dc; nkp += dc; }
     }
 
-    const bool scored_col = !ring && scored_column(a.score, ci, cj);
+    const bool scored_col = !ring && scored_col_t<I>(a.score, ci, cj);
     V4<T> PO, NO;
     T rec_sum = 0, p_sum = 0, n_sum = 0;
 #pragma unroll

@@ -38,6 +38,8 @@ __host__ __device__ constexpr int stream_max_threads(int ipt) {
     return ipt <= 1 ? 17 * 32 : (ipt == 2 ? 13 * 32 : (ipt == 3 ? 11 * 32 : 9 * 32));
 }
 constexpr int kStreamMaxSmem = 227 * 1024;
+// AUTO picks the streaming kernel from this many allocated cells (no_xy^2 * kpitch)
+constexpr int64_t kStreamMinCells = 6000000;
 
 // Launch shape of the streaming step kernel.
 struct StreamShape {
@@ -93,5 +95,10 @@ int batched_loop(const BatchLaunch &L, cudaStream_t st);
 int step_noalloc(const pic_grid *g, const void *pos_in, const void *neg_in, void *pos_out, void *neg_out,
                  const double *xs, const double *ys, int64_t n_tracks, uint32_t *counts, double *tally,
                  cudaStream_t st);
+
+int sample_disc(const double *u, int64_t n_pairs, double scale, double mid, double radius_sq, int64_t n_wanted,
+                double *xs, double *ys, int64_t *n_accepted, int64_t *n_pairs_used);
+int sample_disc_pcg64(uint64_t *st, double scale, double mid, double radius_sq, int64_t n_wanted, int64_t max_pairs,
+                      double *xs, double *ys, int64_t *n_accepted, int64_t *n_draws);
 
 }  // namespace pic

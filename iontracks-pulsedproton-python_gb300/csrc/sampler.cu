@@ -1,0 +1,93 @@
+// sampler.cu -- the rejection step of the track sampler, on the host.
+//
+// The reference draws track centres uniformly in the sampling disc by
+// rejection from consecutive pairs of doubles of its NumPy generator
+// (pulsed_ion_chamber/pulses.py:64-82 per track, :84-171 in blocks):
+//   x = u[2a] * no_xy,  y = u[2a+1] * no_xy,
+//   accepted when (x - mid)^2 + (y - mid)^2 <= radius^2.
+// Two forms:
+//   * sample_disc scans doubles the caller drew from its generator;
+//   * sample_disc_pcg64 draws them itself from the generator's own state when
+//     that generator is NumPy's PCG64 (the default_rng the reference seeds):
+//     the permuted congruential generator of M. E. O'Neill, "PCG: A Family of
+//     Simple Fast Space-Efficient Statistically Good Algorithms for Random
+//     Number Generation" (2014), variant XSL-RR 128/64 -- a 128-bit LCG
+//     state' = state * M + inc, output rotr64(hi(state') ^ lo(state'),
+//     state' >> 122) -- and NumPy's double = (output >> 11) * 2^-53. It draws
+//     exactly the doubles the scan consumes and returns the advanced state, so
+//     the caller's generator continues from the same point as if it had drawn
+//     them.
+// Both stop at the wanted count. The arithmetic is the reference's, one
+// rounding per operation: this file is compiled with -ffp-contract=off so that
+// the sum of squares is never fused into an FMA (which NumPy does not do), on
+// either host architecture.
+#include <stdint.h>
+
+#include "pic_internal.h"
+
+namespace pic {
+
+int sample_disc(const double *u, int64_t n_pairs, double scale, double mid, double radius_sq, int64_t n_wanted,
+                double *xs, double *ys, int64_t *n_accepted, int64_t *n_pairs_used) {
+    int64_t got = 0, a = 0;
+    for (; a < n_pairs && got < n_wanted; ++a) {
+        const double x = u[2 * a] * scale;
+        const double y = u[2 * a + 1] * scale;
+        const double dx = x - mid, dy = y - mid;
+        const double dx2 = dx * dx, dy2 = dy * dy;
+        if (dx2 + dy2 <= radius_sq) {
+            xs[got] = x;
+            ys[got] = y;
+            ++got;
+        }
+    }
+    *n_accepted = got;
+    *n_pairs_used = a;
+    return PIC_OK;
+}
+
+namespace {
+
+typedef unsigned __int128 u128;
+
+// PCG's default 128-bit LCG multiplier.
+constexpr u128 kPcgMult = ((u128)2549297995355413924ULL << 64) | (u128)4865540595714422341ULL;
+
+struct Pcg64 {
+    u128 state, inc;
+    inline uint64_t next() {
+        state = state * kPcgMult + inc;
+        const uint64_t x = (uint64_t)(state >> 64) ^ (uint64_t)state;
+        const unsigned rot = (unsigned)(state >> 122);
+        return (x >> rot) | (x << ((64u - rot) & 63u));
+    }
+    inline double next_double() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }
+};
+
+}  // namespace
+
+int sample_disc_pcg64(uint64_t *st, double scale, double mid, double radius_sq, int64_t n_wanted, int64_t max_pairs,
+                      double *xs, double *ys, int64_t *n_accepted, int64_t *n_draws) {
+    Pcg64 r{((u128)st[0] << 64) | st[1], ((u128)st[2] << 64) | st[3]};
+    int64_t got = 0, draws = 0;
+    // Branch-free accept: every pair is written at the next free slot (in
+    // bounds, since got < n_wanted inside the loop) and the slot is kept only
+    // when accepted -- about a third of the pairs are rejected, at random.
+    while (got < n_wanted && draws < 2 * max_pairs) {
+        const double x = r.next_double() * scale;
+        const double y = r.next_double() * scale;
+        draws += 2;
+        const double dx = x - mid, dy = y - mid;
+        const double dx2 = dx * dx, dy2 = dy * dy;
+        xs[got] = x;
+        ys[got] = y;
+        got += (dx2 + dy2 <= radius_sq) ? 1 : 0;
+    }
+    st[0] = (uint64_t)(r.state >> 64);
+    st[1] = (uint64_t)r.state;
+    *n_accepted = got;
+    *n_draws = draws;
+    return PIC_OK;
+}
+
+}  // namespace pic

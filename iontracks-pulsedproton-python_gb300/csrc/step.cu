@@ -29,14 +29,19 @@
 
 namespace pic {
 
-template <typename T, int BLOCK>
+template <typename T, int BLOCK, typename I>
 __global__ void __launch_bounds__(BLOCK) step_kernel(StepArgs<T> a) {
     Tally<T> t_rec, t_p, t_n, t_inj;
-    const int64_t stride = (int64_t)gridDim.x * BLOCK;
-    for (int64_t item = (int64_t)blockIdx.x * BLOCK + threadIdx.x; item < a.items; item += stride)
-        flat_item(a, item, t_rec, t_p, t_n, t_inj);
-    double v[4] = {t_inj.value(), t_rec.value(), t_p.value(), t_n.value()};
-    finish_tally<BLOCK>(v, a.partials, a.counter, a.tally, a.injected_scale);
+    const I stride = (I)gridDim.x * BLOCK, items = (I)a.items;
+    for (I item = (I)blockIdx.x * BLOCK + threadIdx.x; item < items; item += stride)
+        flat_item<T, I>(a, item, t_rec, t_p, t_n, t_inj);
+    if constexpr (sizeof(T) == 4) {
+        DF v[4] = {df_of(t_inj), df_of(t_rec), df_of(t_p), df_of(t_n)};
+        finish_tally_df<BLOCK>(v, a.partials, a.counter, a.tally, a.injected_scale);
+    } else {
+        double v[4] = {t_inj.value(), t_rec.value(), t_p.value(), t_n.value()};
+        finish_tally<BLOCK>(v, a.partials, a.counter, a.tally, a.injected_scale);
+    }
 }
 
 template <typename T>
@@ -74,7 +79,11 @@ static int launch_step_t(const pic_grid *g, const void *pos_in, const void *neg_
     const int64_t cap = step_grid_cap(g->dtype == PIC_F64 ? 1 : 0);
     if (blocks > cap) blocks = cap;
     if (blocks > kMaxStepBlocks) blocks = kMaxStepBlocks;
-    step_kernel<T, BLOCK><<<(unsigned)blocks, BLOCK, 0, st>>>(a);
+    // (items + stride stays below 2^32 on the 32-bit path: items < 2^29)
+    if (flat_index32(g->no_xy, g->kpitch))
+        step_kernel<T, BLOCK, uint32_t><<<(unsigned)blocks, BLOCK, 0, st>>>(a);
+    else
+        step_kernel<T, BLOCK, int64_t><<<(unsigned)blocks, BLOCK, 0, st>>>(a);
     return check_launch("step_kernel");
 }
 
@@ -95,8 +104,8 @@ int launch_step(const pic_grid *g_in, const void *pos_in, const void *neg_in, vo
 
 int step_occupancy(int dtype, int *blocks_per_sm) {
     cudaError_t e = dtype == PIC_F64
-                        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, step_kernel<double, 256>, 256, 0)
-                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, step_kernel<float, 256>, 256, 0);
+                        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, step_kernel<double, 256, uint32_t>, 256, 0)
+                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, step_kernel<float, 256, uint32_t>, 256, 0);
     return e == cudaSuccess ? PIC_OK : set_cuda_error("cudaOccupancyMaxActiveBlocksPerMultiprocessor", e);
 }
 

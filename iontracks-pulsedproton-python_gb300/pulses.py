@@ -21,7 +21,11 @@ captured CUDA graph.
 
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
+
+from . import _native as N
 
 __all__ = ["build_track_schedule", "TrackSampler", "CylinderSampler", "pulse_arrival_counts"]
 
@@ -33,8 +37,15 @@ def pulse_arrival_counts(config, rng: np.random.Generator) -> np.ndarray:
     arrival = np.cumsum(rng.random(n))
     arrival /= arrival[-1]
     arrival *= config.pulse_duration_s
-    counts, _ = np.histogram(arrival, config.pulse_time_bins)
-    return counts.astype(np.int64)
+    # np.histogram(arrival, bins) over explicit edges counts, per bin, the
+    # values in [edge_b, edge_b+1) (the last bin closed on the right) by binary
+    # searches in the sorted values; arrival is already non-decreasing (a
+    # running sum of non-negative draws, scaled), so the searches run on it
+    # directly and the sort drops out. Same counts, without the O(n log n).
+    bins = np.asarray(config.pulse_time_bins, dtype=np.float64)
+    cum = np.concatenate([np.searchsorted(arrival, bins[:-1], side="left"),
+                          np.searchsorted(arrival, bins[-1:], side="right")])
+    return np.diff(cum).astype(np.int64)
 
 
 def build_track_schedule(config, rng: np.random.Generator) -> np.ndarray:
@@ -61,7 +72,7 @@ class TrackSampler:
 
     _MIN_DRAW = 1 << 13
 
-    def __init__(self, rng: np.random.Generator, mid_xy, radius: float, no_xy: int):
+    def __init__(self, rng: np.random.Generator, mid_xy, radius: float, no_xy: int, native_rng: bool = True):
         self.rng = rng
         self.mid_xy = mid_xy
         self.radius_sq = radius * radius
@@ -69,6 +80,10 @@ class TrackSampler:
         self._accept = min(1.0, max(0.05, np.pi * self.radius_sq / float(no_xy * no_xy)))
         self._buf = np.empty(0)
         self._pos = 0
+        # NumPy's PCG64 (what default_rng gives) is drawn natively from its
+        # state, exactly the doubles consumed; any other bit generator is
+        # drawn through NumPy in blocks and scanned natively.
+        self._pcg64 = native_rng and type(rng.bit_generator) is np.random.PCG64
 
     def _refill(self, wanted: int) -> None:
         pairs = max(self._MIN_DRAW, int(wanted / self._accept * 1.25) + 16)
@@ -77,36 +92,64 @@ class TrackSampler:
         self._pos = 0
 
     def sample(self, n_tracks: int):
-        """``(xs, ys)`` float64 arrays of ``n_tracks`` accepted centres."""
+        """``(xs, ys)`` float64 arrays of ``n_tracks`` accepted centres.
+
+        The doubles come from the generator here; the accept/reject scan over
+        them is the library's ``pic_sample_disc`` (one pass in C, float64,
+        one rounding per operation), which stops at the wanted count.
+        """
         n_tracks = int(n_tracks)
         if n_tracks <= 0:
             return np.empty(0), np.empty(0)
+        if self._pcg64:
+            return self._sample_pcg64(n_tracks)
+        lib = N.load()
         xs_out = np.empty(n_tracks)
         ys_out = np.empty(n_tracks)
+        acc, used = ctypes.c_int64(), ctypes.c_int64()
         filled = 0
         while filled < n_tracks:
             if (self._buf.size - self._pos) < 2:
                 self._refill(n_tracks - filled)
             n_pairs = (self._buf.size - self._pos) // 2
-            block = self._buf[self._pos : self._pos + 2 * n_pairs]
-            x = block[0::2] * self.no_xy
-            y = block[1::2] * self.no_xy
-            ok = (x - self.mid_xy) ** 2 + (y - self.mid_xy) ** 2 <= self.radius_sq
-            idx = np.flatnonzero(ok)
-            need = n_tracks - filled
-            if idx.size >= need:
-                take = idx[:need]
-                used_pairs = int(take[-1]) + 1
-            else:
-                take = idx
-                used_pairs = n_pairs
-            xs_out[filled : filled + take.size] = x[take]
-            ys_out[filled : filled + take.size] = y[take]
-            filled += take.size
-            self._pos += 2 * used_pairs
+            u = self._buf[self._pos :]
+            N.check(lib.pic_sample_disc(u.ctypes.data, n_pairs, float(self.no_xy), float(self.mid_xy),
+                                        float(self.radius_sq), n_tracks - filled,
+                                        xs_out[filled:].ctypes.data, ys_out[filled:].ctypes.data,
+                                        ctypes.byref(acc), ctypes.byref(used)), "pic_sample_disc")
+            filled += acc.value
+            self._pos += 2 * used.value
             if self._pos >= self._buf.size:
                 self._buf = np.empty(0)
                 self._pos = 0
+        return xs_out, ys_out
+
+    def _sample_pcg64(self, n_tracks: int):
+        """Draw and scan in one native pass (``pic_sample_disc_pcg64``) from
+        the generator's PCG64 state, then store the advanced state back: the
+        generator ends exactly past the doubles consumed, so the next call
+        (or any later draw) continues the stream."""
+        lib = N.load()
+        bg = self.rng.bit_generator
+        d = bg.state
+        s, inc = int(d["state"]["state"]), int(d["state"]["inc"])
+        m64 = (1 << 64) - 1
+        st = np.array([s >> 64, s & m64, inc >> 64, inc & m64], dtype=np.uint64)
+        xs_out = np.empty(n_tracks)
+        ys_out = np.empty(n_tracks)
+        acc, draws = ctypes.c_int64(), ctypes.c_int64()
+        filled = 0
+        while filled < n_tracks:
+            # bounded calls keep the interpreter responsive; the stream is
+            # continued across them through st
+            max_pairs = max(1 << 16, int((n_tracks - filled) / self._accept * 1.5) + 1024)
+            N.check(lib.pic_sample_disc_pcg64(st.ctypes.data, float(self.no_xy), float(self.mid_xy),
+                                              float(self.radius_sq), n_tracks - filled, max_pairs,
+                                              xs_out[filled:].ctypes.data, ys_out[filled:].ctypes.data,
+                                              ctypes.byref(acc), ctypes.byref(draws)), "pic_sample_disc_pcg64")
+            filled += acc.value
+        d["state"]["state"] = (int(st[0]) << 64) | int(st[1])
+        bg.state = d
         return xs_out, ys_out
 
 

@@ -119,8 +119,14 @@ def test_launch_shape_resolution_without_a_gpu():
     s = eng.resolve_shape(big)
     assert s["variant"] == "stream"
     assert s["tile_rows"] == 7 and s["consumer_warps"] == 12 and s["stages"] >= 4
+    assert s["planes_per_item"] == 64  # 1066 x 152 tiles: > 12 items per SM even at 64 planes
     small = eng.make_grid(make_config("column_10um_r008"))
     assert eng.resolve_shape(small)["variant"] == "flat"
+    # 208 x 208 x 408 = 17.7 M cells: streaming, with few planes per item so
+    # that 30 j-tiles still give every SM work
+    mid = eng.make_grid(make_config("column_5um_r05_d8p91"))
+    s = eng.resolve_shape(mid)
+    assert s["variant"] == "stream" and 4 <= s["planes_per_item"] <= 8
     f64 = eng.make_grid(make_config("full_electrode_5um_10p"), dtype="float64")
     assert eng.resolve_shape(f64)["variant"] == "flat"
     forced = eng.make_grid(make_config("fast"), shape={"variant": "stream", "tile_rows": 3, "stages": 4})

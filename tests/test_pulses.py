@@ -2,6 +2,7 @@
 bit (pulsed_ion_chamber/pulses.py:39-171), at every configuration size."""
 
 import hashlib
+import importlib
 
 import numpy as np
 import pytest
@@ -51,3 +52,98 @@ def test_schedule_and_first_pulse_tracks_are_bit_identical(name):
     assert list(xs[:8]) == ref["first_pulse_xs_head"]
     assert _sha(xs) == ref["first_pulse_xs_sha256"]
     assert _sha(ys) == ref["first_pulse_ys_sha256"]
+
+
+def _numpy_disc_scan(u, scale, mid, r2, wanted):
+    """The reference's array expression over the uniforms (pulses.py:84-171)."""
+    x = u[0::2] * scale
+    y = u[1::2] * scale
+    idx = np.flatnonzero((x - mid) ** 2 + (y - mid) ** 2 <= r2)[:wanted]
+    return x[idx], y[idx]
+
+
+def test_native_disc_scan_equals_the_numpy_expression():
+    """pic_sample_disc against the NumPy expression on the 64 sweep configs'
+    disc geometries (integer and half-integer centres, radii up to the grid
+    edge) and on draws landing exactly on the disc boundary."""
+    import ctypes
+
+    import importlib
+
+    N = importlib.import_module(pkg().__name__ + "._native")
+    lib = N.load()
+    rng = np.random.default_rng(99)
+    geoms = [(c.no_xy, c.mid_xy, c.sampling_radius) for c in pkg().saturation_sweep_configs()]
+    geoms += [(25, 12.5, 9.5), (60, 30, 24.0), (7, 3.5, 3.5)]
+    for no_xy, mid, rad in geoms:
+        u = rng.random(2 * 5000)
+        u[:8] = [0.5, 0.5, 0.0, 0.0, (mid + rad) / no_xy, mid / no_xy, 0.999999, 0.5]  # centre, corner, boundary
+        for wanted in (1, 37, 10_000):
+            xs, ys = np.empty(wanted), np.empty(wanted)
+            acc, used = ctypes.c_int64(), ctypes.c_int64()
+            N.check(lib.pic_sample_disc(u.ctypes.data, u.size // 2, float(no_xy), float(mid), float(rad * rad),
+                                        wanted, xs.ctypes.data, ys.ctypes.data, ctypes.byref(acc),
+                                        ctypes.byref(used)), "pic_sample_disc")
+            ex, ey = _numpy_disc_scan(u, no_xy, mid, rad * rad, wanted)
+            assert acc.value == len(ex)
+            np.testing.assert_array_equal(xs[: acc.value], ex)
+            np.testing.assert_array_equal(ys[: acc.value], ey)
+            if acc.value == wanted:
+                x = u[0::2] * no_xy
+                y = u[1::2] * no_xy
+                last = used.value - 1
+                assert x[last] == ex[-1] and y[last] == ey[-1]
+            else:
+                assert used.value == u.size // 2
+
+
+def test_arrival_counts_equal_numpy_histogram():
+    """The per-step arrival histogram (binary searches on the sorted arrival
+    times) equals np.histogram over the same edges (pulses.py:39-61), for the
+    golden configurations, the sweep and extra seeds."""
+    cfgs = [make_config(n) for n in NAMES] + pkg().saturation_sweep_configs()
+    for cfg in cfgs:
+        for seed in (cfg.seed, 7):
+            a = importlib.import_module(pkg().__name__ + ".pulses").pulse_arrival_counts(cfg, np.random.default_rng(seed))
+            rng = np.random.default_rng(seed)
+            arrival = np.cumsum(rng.random(int(cfg.number_of_tracks_per_pulse)))
+            arrival /= arrival[-1]
+            arrival *= cfg.pulse_duration_s
+            ref, _ = np.histogram(arrival, cfg.pulse_time_bins)
+            np.testing.assert_array_equal(a, ref)
+
+
+@pytest.mark.parametrize("geom", [(60, 30, 24.0), (25, 12.5, 9.5), (95, 47.5, 43.5), (7, 3.5, 3.5)])
+def test_native_pcg64_draws_equal_numpy_draws(geom):
+    """The PCG64 path (doubles drawn natively from the generator's state)
+    gives the same centres as drawing through NumPy, across uneven and empty
+    batches, and leaves the generator exactly past the doubles consumed."""
+    no_xy, mid, rad = geom
+    a = pkg().TrackSampler(np.random.default_rng(5), mid, rad, no_xy)
+    b = pkg().TrackSampler(np.random.default_rng(5), mid, rad, no_xy, native_rng=False)
+    assert a._pcg64 and not b._pcg64
+    for n in (0, 1, 3, 5000, 0, 17, 100_000, 2):
+        xa, ya = a.sample(n)
+        xb, yb = b.sample(n)
+        np.testing.assert_array_equal(xa, xb)
+        np.testing.assert_array_equal(ya, yb)
+    # the generator sits where a plain NumPy draw of the consumed doubles ends
+    rng = np.random.default_rng(5)
+    ref = pkg().TrackSampler(np.random.default_rng(5), mid, rad, no_xy)
+    xs, ys = ref.sample(1234)
+    consumed = 0
+    u = rng.random(10_000_000)
+    x, y = u[0::2] * no_xy, u[1::2] * no_xy
+    idx = np.flatnonzero((x - mid) ** 2 + (y - mid) ** 2 <= rad * rad)
+    consumed = 2 * (int(idx[1233]) + 1)
+    rng2 = np.random.default_rng(5)
+    rng2.random(consumed)
+    assert ref.rng.random() == rng2.random()
+
+
+def test_other_bit_generators_take_the_numpy_draw_path():
+    g = np.random.Generator(np.random.MT19937(3))
+    s = pkg().TrackSampler(g, 30, 24.0, 60)
+    assert not s._pcg64
+    xs, ys = s.sample(1000)
+    assert np.all((xs - 30) ** 2 + (ys - 30) ** 2 <= 24.0**2)
