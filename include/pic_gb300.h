@@ -203,6 +203,54 @@ int pic_sample_disc_pcg64(uint64_t *state, double scale, double mid, double radi
                           int64_t max_pairs, double *xs, double *ys, int64_t *n_accepted, int64_t *n_draws);
 
 /*
+ * Adjoint of the fused step (no counterpart in the reference, which has no
+ * derivatives): reverse-mode derivatives of R, the run's total recombined
+ * charge, for k_s = I / (I - R).
+ *
+ * pic_adjoint_step -- one step backwards. Given the state u_s that step s
+ * read (pos/neg), its 2D density (dens, or NULL when the step deposited
+ * nothing) and lambda_{s+1} = dR/du_{s+1} (lam_*_in), writes
+ * lambda_s = dR/du_s (lam_*_out) and grad[0..4] = this step's contribution to
+ * dR/ds+, dR/dc+, dR/ds-, dR/dc-, dR/d(alpha_dt), where s = D dt / h^2 and
+ * c = mu E dt / h are each species' diffusion and Courant numbers (the
+ * descriptor's weights are lat = s, zm = s + c(c+1)/2, zp = s + c(c-1)/2,
+ * cen = 1 - c^2 - 6s), at fixed dt. Reflecting wall: lam_*_in
+ * is modified (the ring's adjoint is folded into the interior columns it
+ * copies). Workspace: pic_adjoint_workspace_bytes, zeroed once.
+ */
+int pic_adjoint_workspace_bytes(const pic_grid *g, int64_t *bytes);
+int pic_adjoint_step(const pic_grid *g, const void *pos, const void *neg, const void *dens, void *lam_pos_in,
+                     void *lam_neg_in, void *lam_pos_out, void *lam_neg_out, double *grad, void *workspace,
+                     int64_t workspace_bytes, uintptr_t stream);
+
+/*
+ * pic_forward_states -- n_steps steps forward from state 0 of a state array,
+ * keeping every state: step s reads state s and writes state s + 1, where
+ * state s is pos_states/neg_states + s * state_stride elements
+ * (state_stride >= no_xy^2 * kpitch, a multiple of 8). Step s deposits tracks
+ * [track_offsets[s], track_offsets[s+1]) of xs/ys into its own density slot
+ * s of dens_states ([n_steps][no_xy][pic_dens_pitch], cleared here first),
+ * updating counts; tallies go to tally[4*s .. 4*s+3]. Workspace as pic_step.
+ * The recomputation half of a checkpointed reverse sweep.
+ */
+int pic_forward_states(const pic_grid *g, void *pos_states, void *neg_states, int64_t state_stride, int64_t n_steps,
+                       const double *xs, const double *ys, const int64_t *track_offsets, void *dens_states,
+                       uint32_t *counts, double *tally, void *workspace, int64_t workspace_bytes, uintptr_t stream);
+
+/*
+ * pic_adjoint_segment -- the adjoint steps s = n_steps-1 .. 0 over the states
+ * and densities pic_forward_states kept (a step with no tracks reads no
+ * density). lambda_{n_steps} is in buffer lam_parity of (lam_*0, lam_*1) on
+ * entry; each step writes the other buffer, so lambda_0 ends in buffer
+ * (lam_parity + n_steps) & 1. grad_rows[5*s .. 5*s+4] receives step s's
+ * gradients (as pic_adjoint_step).
+ */
+int pic_adjoint_segment(const pic_grid *g, const void *pos_states, const void *neg_states, int64_t state_stride,
+                        const void *dens_states, const int64_t *track_offsets, int64_t n_steps, void *lam_pos0,
+                        void *lam_neg0, void *lam_pos1, void *lam_neg1, int64_t lam_parity, double *grad_rows,
+                        void *workspace, int64_t workspace_bytes, uintptr_t stream);
+
+/*
  * pic_run_segment -- n_steps consecutive time steps on the device.
  *
  * Step s (0-based within the segment) reads fields[(parity + s) & 1] and

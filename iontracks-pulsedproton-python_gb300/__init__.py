@@ -27,6 +27,10 @@ __all__ = [
     "run_simulation_b200",
     "run_batched_b200",
     "saturation_sweep_configs",
+    "ks_b200",
+    "ks_and_gradient",
+    "fit_alpha",
+    "AdjointRun",
 ]
 
 
@@ -41,4 +45,8 @@ def __getattr__(name):
         from . import batched
 
         return getattr(batched, name)
+    if name in ("ks_b200", "ks_and_gradient", "fit_alpha", "AdjointRun"):
+        from . import adjoint
+
+        return getattr(adjoint, name)
     raise AttributeError(name)

@@ -343,6 +343,101 @@ int pic_sample_disc_pcg64(uint64_t *state, double scale, double mid, double radi
     return sample_disc_pcg64(state, scale, mid, radius_sq, n_wanted, max_pairs, xs, ys, n_accepted, n_draws);
 }
 
+int pic_adjoint_workspace_bytes(const pic_grid *g, int64_t *bytes) {
+    int rc = check_grid(g);
+    if (rc) return rc;
+    if (!bytes) return set_error(PIC_E_INVALID, "bytes is null");
+    return adjoint_workspace_bytes(bytes);
+}
+
+int pic_adjoint_step(const pic_grid *g, const void *pos, const void *neg, const void *dens, void *lam_pos_in,
+                     void *lam_neg_in, void *lam_pos_out, void *lam_neg_out, double *grad, void *workspace,
+                     int64_t workspace_bytes, uintptr_t stream) {
+    int rc = check_grid(g);
+    if (rc) return rc;
+    if ((rc = check_fields(pos, neg, lam_pos_in, lam_neg_in)) || (rc = check_fields(lam_pos_out, lam_neg_out, pos, neg)))
+        return rc;
+    if (lam_pos_in == lam_pos_out || lam_neg_in == lam_neg_out)
+        return set_error(PIC_E_INVALID, "adjoint input and output buffers must differ");
+    if (!grad) return set_error(PIC_E_INVALID, "grad is null");
+    int64_t need = 0;
+    adjoint_workspace_bytes(&need);
+    if (!workspace || workspace_bytes < need) return set_error(PIC_E_INVALID, "workspace too small (pic_adjoint_workspace_bytes)");
+    return launch_adjoint(g, pos, neg, dens, lam_pos_in, lam_neg_in, lam_pos_out, lam_neg_out, grad, workspace,
+                          reinterpret_cast<cudaStream_t>(stream));
+}
+
+int pic_forward_states(const pic_grid *g, void *pos_states, void *neg_states, int64_t state_stride, int64_t n_steps,
+                       const double *xs, const double *ys, const int64_t *track_offsets, void *dens_states,
+                       uint32_t *counts, double *tally, void *workspace, int64_t workspace_bytes, uintptr_t stream) {
+    int rc = check_grid(g);
+    if (rc) return rc;
+    if (n_steps < 0) return set_error(PIC_E_INVALID, "n_steps must be >= 0");
+    if (n_steps == 0) return PIC_OK;
+    if (!track_offsets || !dens_states || !counts || !tally) return set_error(PIC_E_INVALID, "null pointer argument");
+    if ((rc = check_fields(pos_states, neg_states, pos_states, neg_states))) return rc;
+    if (!aligned(dens_states, 16)) return set_error(PIC_E_INVALID, "dens_states must be 16-byte aligned");
+    const int64_t field = g->no_xy * g->no_xy * g->kpitch;
+    if (state_stride < field || state_stride % 8 != 0)
+        return set_error(PIC_E_INVALID, "state_stride must be >= no_xy^2 * kpitch and a multiple of 8 elements");
+    if (!workspace || workspace_bytes < kWorkspaceBytes)
+        return set_error(PIC_E_INVALID, "workspace too small (pic_step_workspace_bytes)");
+    for (int64_t s = 0; s < n_steps; ++s)
+        if (track_offsets[s + 1] < track_offsets[s]) return set_error(PIC_E_INVALID, "track_offsets must be non-decreasing");
+    if (track_offsets[n_steps] > track_offsets[0] && (!xs || !ys)) return set_error(PIC_E_INVALID, "track arrays are null");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const int64_t es = g->dtype == PIC_F64 ? 8 : 4;
+    const int64_t dslot = g->no_xy * dens_pitch(g->no_xy);
+    cudaError_t e = cudaMemsetAsync(dens_states, 0, (size_t)(n_steps * dslot * es), st);
+    if (e != cudaSuccess) return set_cuda_error("cudaMemsetAsync(dens_states)", e);
+    char *P = static_cast<char *>(pos_states), *N = static_cast<char *>(neg_states);
+    char *D = static_cast<char *>(dens_states);
+    for (int64_t s = 0; s < n_steps; ++s) {
+        const int64_t m = track_offsets[s + 1] - track_offsets[s];
+        void *dens = D + s * dslot * es;
+        if (m > 0 && (rc = launch_deposit(g, xs + track_offsets[s], ys + track_offsets[s], m, dens, counts, st)))
+            return rc;
+        rc = launch_step(g, P + s * state_stride * es, N + s * state_stride * es, P + (s + 1) * state_stride * es,
+                         N + (s + 1) * state_stride * es, m > 0 ? dens : nullptr, nullptr, tally + 4 * s, workspace, st);
+        if (rc) return rc;
+    }
+    return PIC_OK;
+}
+
+int pic_adjoint_segment(const pic_grid *g, const void *pos_states, const void *neg_states, int64_t state_stride,
+                        const void *dens_states, const int64_t *track_offsets, int64_t n_steps, void *lam_pos0,
+                        void *lam_neg0, void *lam_pos1, void *lam_neg1, int64_t lam_parity, double *grad_rows,
+                        void *workspace, int64_t workspace_bytes, uintptr_t stream) {
+    int rc = check_grid(g);
+    if (rc) return rc;
+    if (n_steps < 0) return set_error(PIC_E_INVALID, "n_steps must be >= 0");
+    if (n_steps == 0) return PIC_OK;
+    if (!track_offsets || !dens_states || !grad_rows) return set_error(PIC_E_INVALID, "null pointer argument");
+    if ((rc = check_fields(pos_states, neg_states, pos_states, neg_states))) return rc;
+    if ((rc = check_fields(lam_pos0, lam_neg0, lam_pos1, lam_neg1))) return rc;
+    const int64_t field = g->no_xy * g->no_xy * g->kpitch;
+    if (state_stride < field || state_stride % 8 != 0)
+        return set_error(PIC_E_INVALID, "state_stride must be >= no_xy^2 * kpitch and a multiple of 8 elements");
+    int64_t need = 0;
+    adjoint_workspace_bytes(&need);
+    if (!workspace || workspace_bytes < need) return set_error(PIC_E_INVALID, "workspace too small (pic_adjoint_workspace_bytes)");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const int64_t es = g->dtype == PIC_F64 ? 8 : 4;
+    const int64_t dslot = g->no_xy * dens_pitch(g->no_xy);
+    const char *P = static_cast<const char *>(pos_states), *N = static_cast<const char *>(neg_states);
+    const char *D = static_cast<const char *>(dens_states);
+    void *lp[2] = {lam_pos0, lam_pos1}, *ln[2] = {lam_neg0, lam_neg1};
+    int cur = (int)(lam_parity & 1);  // holds lambda_{s+1}
+    for (int64_t s = n_steps - 1; s >= 0; --s) {
+        const int64_t m = track_offsets[s + 1] - track_offsets[s];
+        rc = launch_adjoint(g, P + s * state_stride * es, N + s * state_stride * es, m > 0 ? D + s * dslot * es : nullptr,
+                            lp[cur], ln[cur], lp[cur ^ 1], ln[cur ^ 1], grad_rows + 5 * s, workspace, st);
+        if (rc) return rc;
+        cur ^= 1;
+    }
+    return PIC_OK;
+}
+
 int pic_run_segment(const pic_grid *g, void *pos0, void *neg0, void *pos1, void *neg1, int64_t parity,
                     int64_t n_steps, const double *xs, const double *ys, const int64_t *track_offsets,
                     void *dens0, void *dens1, int64_t dens_parity, uint32_t *counts, double *tally,
