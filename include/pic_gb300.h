@@ -224,31 +224,39 @@ int pic_adjoint_step(const pic_grid *g, const void *pos, const void *neg, const 
                      int64_t workspace_bytes, uintptr_t stream);
 
 /*
- * pic_forward_states -- n_steps steps forward from state 0 of a state array,
- * keeping every state: step s reads state s and writes state s + 1, where
- * state s is pos_states/neg_states + s * state_stride elements
- * (state_stride >= no_xy^2 * kpitch, a multiple of 8). Step s deposits tracks
- * [track_offsets[s], track_offsets[s+1]) of xs/ys into its own density slot
- * s of dens_states ([n_steps][no_xy][pic_dens_pitch], cleared here first),
- * updating counts; tallies go to tally[4*s .. 4*s+3]. Workspace as pic_step.
- * The recomputation half of a checkpointed reverse sweep.
+ * pic_adjoint_forward -- the forward pass of a checkpointed gradient:
+ * n_steps steps over the field pair (state s in (pos0, neg0) for even s,
+ * (pos1, neg1) for odd s; state 0 in pair 0 on entry), tallies into
+ * tally[4*s ..], the track histogram into counts. Before step
+ * c * ckpt_every it copies the state into checkpoint c
+ * (ckpt_pos/neg + c * state_stride elements; state_stride >= no_xy^2 *
+ * kpitch, a multiple of 8). Every step with tracks keeps its 2D density: the
+ * d-th such step deposits into slot d of dens_keep
+ * ([n_dep][no_xy][pic_dens_pitch], cleared here first), which the backward
+ * pass reads instead of depositing again. Workspace as pic_step.
  */
-int pic_forward_states(const pic_grid *g, void *pos_states, void *neg_states, int64_t state_stride, int64_t n_steps,
-                       const double *xs, const double *ys, const int64_t *track_offsets, void *dens_states,
-                       uint32_t *counts, double *tally, void *workspace, int64_t workspace_bytes, uintptr_t stream);
+int pic_adjoint_forward(const pic_grid *g, void *pos0, void *neg0, void *pos1, void *neg1, int64_t n_steps,
+                        const double *xs, const double *ys, const int64_t *track_offsets, void *dens_keep,
+                        uint32_t *counts, double *tally, void *ckpt_pos, void *ckpt_neg, int64_t ckpt_every,
+                        int64_t state_stride, void *workspace, int64_t workspace_bytes, uintptr_t stream);
 
 /*
- * pic_adjoint_segment -- the adjoint steps s = n_steps-1 .. 0 over the states
- * and densities pic_forward_states kept (a step with no tracks reads no
- * density). lambda_{n_steps} is in buffer lam_parity of (lam_*0, lam_*1) on
- * entry; each step writes the other buffer, so lambda_0 ends in buffer
- * (lam_parity + n_steps) & 1. grad_rows[5*s .. 5*s+4] receives step s's
- * gradients (as pic_adjoint_step).
+ * pic_adjoint_backward -- the reverse sweep: for each checkpoint segment from
+ * the last, recompute the segment's states from its checkpoint into
+ * states_pos/neg (ckpt_every states, state_stride apart; kept densities, no
+ * deposition; tallies to the 4-double tally_scratch), then run the adjoint
+ * steps over them backwards. lambda starts at zero in buffer 0 of
+ * (lam_*0, lam_*1) (both zeroed by the caller); lambda_0 ends in buffer
+ * n_steps & 1. grad_rows[5*s .. 5*s+4] receives step s's
+ * dR/d(s+, c+, s-, c-, alpha_dt) (as pic_adjoint_step). Workspaces: the
+ * step's (pic_step_workspace_bytes) and the adjoint's
+ * (pic_adjoint_workspace_bytes), each zeroed once.
  */
-int pic_adjoint_segment(const pic_grid *g, const void *pos_states, const void *neg_states, int64_t state_stride,
-                        const void *dens_states, const int64_t *track_offsets, int64_t n_steps, void *lam_pos0,
-                        void *lam_neg0, void *lam_pos1, void *lam_neg1, int64_t lam_parity, double *grad_rows,
-                        void *workspace, int64_t workspace_bytes, uintptr_t stream);
+int pic_adjoint_backward(const pic_grid *g, const void *ckpt_pos, const void *ckpt_neg, int64_t state_stride,
+                         int64_t n_steps, int64_t ckpt_every, const int64_t *track_offsets, const void *dens_keep,
+                         void *states_pos, void *states_neg, void *lam_pos0, void *lam_neg0, void *lam_pos1,
+                         void *lam_neg1, double *grad_rows, double *tally_scratch, void *workspace,
+                         int64_t workspace_bytes, void *adj_workspace, int64_t adj_workspace_bytes, uintptr_t stream);
 
 /*
  * pic_run_segment -- n_steps consecutive time steps on the device.

@@ -20,13 +20,14 @@ reference give away from a rung.
 
 Method (reverse mode with checkpoints):
 
-1. forward: the float32 (or float64) run of :func:`run_simulation_b200`, step
-   by step on the device, storing the state every ``checkpoint_every`` steps;
-2. backward, one segment of ``checkpoint_every`` steps at a time from the
-   last: recompute the segment's states from its checkpoint
-   (``pic_forward_states``), then run the adjoint steps backwards over them
-   (``pic_adjoint_segment``), carrying ``lambda = dR/du`` across segments and
-   summing each step's ``dR/ds+, dR/dc+, dR/ds-, dR/dc-, dR/da``;
+1. forward (``pic_adjoint_forward``): the float32 (or float64) run of
+   :func:`run_simulation_b200`, storing the state every ``checkpoint_every``
+   steps and keeping each depositing step's 2D density;
+2. backward (``pic_adjoint_backward``), one segment of ``checkpoint_every``
+   steps at a time from the last: recompute the segment's states from its
+   checkpoint with the kept densities, then run the adjoint steps backwards
+   over them, carrying ``lambda = dR/du`` across segments and recording each
+   step's ``dR/ds+, dR/dc+, dR/ds-, dR/dc-, dR/da``;
 3. the chain rule to the six parameters, in float64 on the host.
 
 ``dk_s/dtheta = k_s^2 / I * dR/dtheta``.
@@ -85,8 +86,9 @@ class AdjointRun:
 
     ``theta`` = (alpha, mu+, mu-, D+, D-, V) (default: the configuration's
     own, with the reference's alpha). ``checkpoint_every`` = steps between
-    stored states (memory: one state per checkpoint plus a segment buffer of
-    ``checkpoint_every + 1`` states and as many 2D densities).
+    stored states (memory: one state per checkpoint, a segment buffer of
+    ``checkpoint_every`` states, and the 2D density of every step with
+    tracks).
     """
 
     def __init__(self, config, theta=None, checkpoint_every: int = 64, dtype: str = "float32", rng=None):
@@ -129,19 +131,32 @@ class AdjointRun:
         g.alpha_dt = adt
         eng.upload_tracks(xs, ys)
         self._eng = eng
-        n_seg = -(-total // self.K)
+        self.n_seg = -(-total // self.K)
         field = int(g.no_xy) ** 2 * int(g.kpitch)
         self.field = field
-        tdt = eng.pos[0].dtype
-        self.ckpt = torch.empty((max(n_seg, 1), 2, field), dtype=tdt, device=eng.device)
-        for c in range(n_seg):
-            s0, s1 = c * self.K, min(total, (c + 1) * self.K)
-            self.ckpt[c, 0].copy_(eng.pos[eng.parity].view(-1))
-            self.ckpt[c, 1].copy_(eng.neg[eng.parity].view(-1))
-            eng.run_segment(self.offsets[s0 : s1 + 1] - self.offsets[s0], track_base=int(self.offsets[s0]))
-        torch.cuda.synchronize(eng.device)
-        eng.check_status()
+        dev, tdt = eng.device, eng.pos[0].dtype
+        n = int(g.no_xy)
+        self.dslot = n * ((n + 3) // 4 * 4)
+        n_dep = int(np.count_nonzero(schedule))
+        es = 4 if self.dtype == "float32" else 8
+        need = (self.n_seg + self.K) * 2 * field * es + n_dep * self.dslot * es + 4 * field * es
+        free, _ = torch.cuda.mem_get_info(dev)
+        if need > 0.9 * free:
+            raise MemoryError(f"the gradient needs {need / 2**30:.2f} GiB of device memory for checkpoints, "
+                              f"the segment buffer and the kept densities; {free / 2**30:.2f} GiB is free "
+                              f"(raise checkpoint_every to trade memory for recomputation)")
+        self.ckpt = torch.empty((2, max(self.n_seg, 1), field), dtype=tdt, device=dev)
+        self.dens_keep = torch.empty((max(n_dep, 1), self.dslot), dtype=tdt, device=dev)
+        st = torch.cuda.current_stream(dev).cuda_stream
+        off = np.ascontiguousarray(self.offsets)
+        N.check(self.lib.pic_adjoint_forward(
+            ctypes.byref(g), eng.pos[0].data_ptr(), eng.neg[0].data_ptr(), eng.pos[1].data_ptr(),
+            eng.neg[1].data_ptr(), total, eng.xs.data_ptr(), eng.ys.data_ptr(), off.ctypes.data_as(ctypes.c_void_p),
+            self.dens_keep.data_ptr(), eng.counts.data_ptr(), eng.tally.data_ptr(), self.ckpt[0].data_ptr(),
+            self.ckpt[1].data_ptr(), self.K, field, eng.workspace.data_ptr(), eng.workspace.numel(), st),
+            "pic_adjoint_forward")
         tallies = eng.tallies(total)
+        eng.check_status()
         # running float64 totals, as the solver and the reference form them
         self.injected = float(np.cumsum(tallies[:, 0])[-1])
         self.recombined = float(np.cumsum(tallies[:, 1])[-1])
@@ -162,40 +177,23 @@ class AdjointRun:
         total = int(self.config.total_time_steps)
         K, field = self.K, self.field
         dev, tdt = eng.device, eng.pos[0].dtype
-        n, dp = int(g.no_xy), (int(g.no_xy) + 3) // 4 * 4
-        states = torch.empty((2, K + 1, field), dtype=tdt, device=dev)
-        dens = torch.empty((K, n * dp), dtype=tdt, device=dev)
-        lam = [torch.zeros((2, field), dtype=tdt, device=dev) for _ in range(2)]
+        states = torch.empty((2, K, field), dtype=tdt, device=dev)
+        lam = torch.zeros((2, 2, field), dtype=tdt, device=dev)  # [buffer][species]
         grad_rows = torch.zeros((max(total, 1), 5), dtype=torch.float64, device=dev)
-        counts = torch.zeros(n * n, dtype=torch.int32, device=dev)
-        tally = torch.zeros((K, 4), dtype=torch.float64, device=dev)
+        scratch = torch.zeros(4, dtype=torch.float64, device=dev)
         awb = ctypes.c_int64()
         N.check(lib.pic_adjoint_workspace_bytes(ctypes.byref(g), ctypes.byref(awb)), "pic_adjoint_workspace_bytes")
         adj_ws = torch.zeros(int(awb.value), dtype=torch.uint8, device=dev)
         st = torch.cuda.current_stream(dev).cuda_stream
-        parity = 0
-        n_seg = -(-total // K)
-        for c in range(n_seg - 1, -1, -1):
-            s0, s1 = c * K, min(total, (c + 1) * K)
-            L = s1 - s0
-            off = np.ascontiguousarray(self.offsets[s0 : s1 + 1] - self.offsets[s0])
-            states[0, 0].copy_(self.ckpt[c, 0])
-            states[1, 0].copy_(self.ckpt[c, 1])
-            base = 8 * int(self.offsets[s0])
-            N.check(lib.pic_forward_states(
-                ctypes.byref(g), states[0].data_ptr(), states[1].data_ptr(), field, L,
-                eng.xs.data_ptr() + base, eng.ys.data_ptr() + base, off.ctypes.data_as(ctypes.c_void_p),
-                dens.data_ptr(), counts.data_ptr(), tally.data_ptr(), eng.workspace.data_ptr(),
-                eng.workspace.numel(), st), "pic_forward_states")
-            N.check(lib.pic_adjoint_segment(
-                ctypes.byref(g), states[0].data_ptr(), states[1].data_ptr(), field, dens.data_ptr(),
-                off.ctypes.data_as(ctypes.c_void_p), L, lam[0][0].data_ptr(), lam[0][1].data_ptr(),
-                lam[1][0].data_ptr(), lam[1][1].data_ptr(), parity, grad_rows[s0].data_ptr(), adj_ws.data_ptr(),
-                adj_ws.numel(), st), "pic_adjoint_segment")
-            parity = (parity + L) & 1
-        torch.cuda.synchronize(dev)
-        eng.check_status()
+        off = np.ascontiguousarray(self.offsets)
+        N.check(lib.pic_adjoint_backward(
+            ctypes.byref(g), self.ckpt[0].data_ptr(), self.ckpt[1].data_ptr(), field, total, K,
+            off.ctypes.data_as(ctypes.c_void_p), self.dens_keep.data_ptr(), states[0].data_ptr(),
+            states[1].data_ptr(), lam[0, 0].data_ptr(), lam[0, 1].data_ptr(), lam[1, 0].data_ptr(),
+            lam[1, 1].data_ptr(), grad_rows.data_ptr(), scratch.data_ptr(), eng.workspace.data_ptr(),
+            eng.workspace.numel(), adj_ws.data_ptr(), adj_ws.numel(), st), "pic_adjoint_backward")
         rows = grad_rows[:total].cpu().numpy()
+        eng.check_status()
         self.timings["backward_s"] = perf_counter() - t0
         return rows.sum(axis=0)
 
@@ -226,6 +224,7 @@ class AdjointRun:
             self._eng.close()
             self._eng = None
         self.ckpt = None
+        self.dens_keep = None
 
 
 def ks_and_gradient(config, theta=None, checkpoint_every: int = 64, dtype: str = "float32", rng=None):

@@ -367,73 +367,130 @@ int pic_adjoint_step(const pic_grid *g, const void *pos, const void *neg, const 
                           reinterpret_cast<cudaStream_t>(stream));
 }
 
-int pic_forward_states(const pic_grid *g, void *pos_states, void *neg_states, int64_t state_stride, int64_t n_steps,
-                       const double *xs, const double *ys, const int64_t *track_offsets, void *dens_states,
-                       uint32_t *counts, double *tally, void *workspace, int64_t workspace_bytes, uintptr_t stream) {
+// Slots of the kept densities: the d-th step with tracks uses slot d.
+static int kept_slots(const int64_t *off, int64_t n_steps, int64_t *n_dep) {
+    int64_t d = 0;
+    for (int64_t s = 0; s < n_steps; ++s) {
+        if (off[s + 1] < off[s]) return set_error(PIC_E_INVALID, "track_offsets must be non-decreasing");
+        d += off[s + 1] > off[s];
+    }
+    *n_dep = d;
+    return PIC_OK;
+}
+
+int pic_adjoint_forward(const pic_grid *g, void *pos0, void *neg0, void *pos1, void *neg1, int64_t n_steps,
+                        const double *xs, const double *ys, const int64_t *track_offsets, void *dens_keep,
+                        uint32_t *counts, double *tally, void *ckpt_pos, void *ckpt_neg, int64_t ckpt_every,
+                        int64_t state_stride, void *workspace, int64_t workspace_bytes, uintptr_t stream) {
     int rc = check_grid(g);
     if (rc) return rc;
-    if (n_steps < 0) return set_error(PIC_E_INVALID, "n_steps must be >= 0");
-    if (n_steps == 0) return PIC_OK;
-    if (!track_offsets || !dens_states || !counts || !tally) return set_error(PIC_E_INVALID, "null pointer argument");
-    if ((rc = check_fields(pos_states, neg_states, pos_states, neg_states))) return rc;
-    if (!aligned(dens_states, 16)) return set_error(PIC_E_INVALID, "dens_states must be 16-byte aligned");
+    if ((rc = check_fields(pos0, neg0, pos1, neg1)) || (rc = check_fields(ckpt_pos, ckpt_neg, ckpt_pos, ckpt_neg)))
+        return rc;
+    if (n_steps < 0 || ckpt_every < 1) return set_error(PIC_E_INVALID, "n_steps must be >= 0 and ckpt_every >= 1");
+    if (!track_offsets || !counts || !tally) return set_error(PIC_E_INVALID, "null pointer argument");
     const int64_t field = g->no_xy * g->no_xy * g->kpitch;
     if (state_stride < field || state_stride % 8 != 0)
         return set_error(PIC_E_INVALID, "state_stride must be >= no_xy^2 * kpitch and a multiple of 8 elements");
     if (!workspace || workspace_bytes < kWorkspaceBytes)
         return set_error(PIC_E_INVALID, "workspace too small (pic_step_workspace_bytes)");
-    for (int64_t s = 0; s < n_steps; ++s)
-        if (track_offsets[s + 1] < track_offsets[s]) return set_error(PIC_E_INVALID, "track_offsets must be non-decreasing");
-    if (track_offsets[n_steps] > track_offsets[0] && (!xs || !ys)) return set_error(PIC_E_INVALID, "track arrays are null");
+    int64_t n_dep = 0;
+    if ((rc = kept_slots(track_offsets, n_steps, &n_dep))) return rc;
+    if (n_dep > 0 && (!xs || !ys || !dens_keep)) return set_error(PIC_E_INVALID, "track or density arrays are null");
+    if (n_dep > 0 && !aligned(dens_keep, 16)) return set_error(PIC_E_INVALID, "dens_keep must be 16-byte aligned");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     const int64_t es = g->dtype == PIC_F64 ? 8 : 4;
     const int64_t dslot = g->no_xy * dens_pitch(g->no_xy);
-    cudaError_t e = cudaMemsetAsync(dens_states, 0, (size_t)(n_steps * dslot * es), st);
-    if (e != cudaSuccess) return set_cuda_error("cudaMemsetAsync(dens_states)", e);
-    char *P = static_cast<char *>(pos_states), *N = static_cast<char *>(neg_states);
-    char *D = static_cast<char *>(dens_states);
+    if (n_dep > 0) {
+        cudaError_t e = cudaMemsetAsync(dens_keep, 0, (size_t)(n_dep * dslot * es), st);
+        if (e != cudaSuccess) return set_cuda_error("cudaMemsetAsync(dens_keep)", e);
+    }
+    void *pos[2] = {pos0, pos1}, *neg[2] = {neg0, neg1};
+    char *D = static_cast<char *>(dens_keep);
+    int64_t d = 0;
     for (int64_t s = 0; s < n_steps; ++s) {
+        const int b = (int)(s & 1);
+        if (s % ckpt_every == 0) {
+            const int64_t c = s / ckpt_every;
+            cudaError_t e = cudaMemcpyAsync(static_cast<char *>(ckpt_pos) + c * state_stride * es, pos[b],
+                                            (size_t)(field * es), cudaMemcpyDeviceToDevice, st);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(static_cast<char *>(ckpt_neg) + c * state_stride * es, neg[b],
+                                    (size_t)(field * es), cudaMemcpyDeviceToDevice, st);
+            if (e != cudaSuccess) return set_cuda_error("cudaMemcpyAsync(checkpoint)", e);
+        }
         const int64_t m = track_offsets[s + 1] - track_offsets[s];
-        void *dens = D + s * dslot * es;
-        if (m > 0 && (rc = launch_deposit(g, xs + track_offsets[s], ys + track_offsets[s], m, dens, counts, st)))
-            return rc;
-        rc = launch_step(g, P + s * state_stride * es, N + s * state_stride * es, P + (s + 1) * state_stride * es,
-                         N + (s + 1) * state_stride * es, m > 0 ? dens : nullptr, nullptr, tally + 4 * s, workspace, st);
+        void *dens = nullptr;
+        if (m > 0) {
+            dens = D + (d++) * dslot * es;
+            if ((rc = launch_deposit(g, xs + track_offsets[s], ys + track_offsets[s], m, dens, counts, st))) return rc;
+        }
+        rc = launch_step(g, pos[b], neg[b], pos[b ^ 1], neg[b ^ 1], dens, nullptr, tally + 4 * s, workspace, st);
         if (rc) return rc;
     }
     return PIC_OK;
 }
 
-int pic_adjoint_segment(const pic_grid *g, const void *pos_states, const void *neg_states, int64_t state_stride,
-                        const void *dens_states, const int64_t *track_offsets, int64_t n_steps, void *lam_pos0,
-                        void *lam_neg0, void *lam_pos1, void *lam_neg1, int64_t lam_parity, double *grad_rows,
-                        void *workspace, int64_t workspace_bytes, uintptr_t stream) {
+int pic_adjoint_backward(const pic_grid *g, const void *ckpt_pos, const void *ckpt_neg, int64_t state_stride,
+                         int64_t n_steps, int64_t ckpt_every, const int64_t *track_offsets, const void *dens_keep,
+                         void *states_pos, void *states_neg, void *lam_pos0, void *lam_neg0, void *lam_pos1,
+                         void *lam_neg1, double *grad_rows, double *tally_scratch, void *workspace,
+                         int64_t workspace_bytes, void *adj_workspace, int64_t adj_workspace_bytes, uintptr_t stream) {
     int rc = check_grid(g);
     if (rc) return rc;
-    if (n_steps < 0) return set_error(PIC_E_INVALID, "n_steps must be >= 0");
-    if (n_steps == 0) return PIC_OK;
-    if (!track_offsets || !dens_states || !grad_rows) return set_error(PIC_E_INVALID, "null pointer argument");
-    if ((rc = check_fields(pos_states, neg_states, pos_states, neg_states))) return rc;
-    if ((rc = check_fields(lam_pos0, lam_neg0, lam_pos1, lam_neg1))) return rc;
+    if ((rc = check_fields(ckpt_pos, ckpt_neg, states_pos, states_neg)) ||
+        (rc = check_fields(lam_pos0, lam_neg0, lam_pos1, lam_neg1)))
+        return rc;
+    if (n_steps < 0 || ckpt_every < 1) return set_error(PIC_E_INVALID, "n_steps must be >= 0 and ckpt_every >= 1");
+    if (!track_offsets || !grad_rows || !tally_scratch) return set_error(PIC_E_INVALID, "null pointer argument");
     const int64_t field = g->no_xy * g->no_xy * g->kpitch;
     if (state_stride < field || state_stride % 8 != 0)
         return set_error(PIC_E_INVALID, "state_stride must be >= no_xy^2 * kpitch and a multiple of 8 elements");
+    if (!workspace || workspace_bytes < kWorkspaceBytes)
+        return set_error(PIC_E_INVALID, "workspace too small (pic_step_workspace_bytes)");
     int64_t need = 0;
     adjoint_workspace_bytes(&need);
-    if (!workspace || workspace_bytes < need) return set_error(PIC_E_INVALID, "workspace too small (pic_adjoint_workspace_bytes)");
+    if (!adj_workspace || adj_workspace_bytes < need)
+        return set_error(PIC_E_INVALID, "adjoint workspace too small (pic_adjoint_workspace_bytes)");
+    int64_t n_dep = 0;
+    if ((rc = kept_slots(track_offsets, n_steps, &n_dep))) return rc;
+    if (n_dep > 0 && !dens_keep) return set_error(PIC_E_INVALID, "dens_keep is null");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     const int64_t es = g->dtype == PIC_F64 ? 8 : 4;
     const int64_t dslot = g->no_xy * dens_pitch(g->no_xy);
-    const char *P = static_cast<const char *>(pos_states), *N = static_cast<const char *>(neg_states);
-    const char *D = static_cast<const char *>(dens_states);
+    const char *D = static_cast<const char *>(dens_keep);
+    char *SP = static_cast<char *>(states_pos), *SN = static_cast<char *>(states_neg);
+    // slot of every step's kept density (-1: none)
+    std::vector<int64_t> slot(n_steps > 0 ? n_steps : 1);
+    {
+        int64_t d = 0;
+        for (int64_t s = 0; s < n_steps; ++s) slot[s] = track_offsets[s + 1] > track_offsets[s] ? d++ : -1;
+    }
+    auto dens_of = [&](int64_t s) -> const void * { return slot[s] < 0 ? nullptr : D + slot[s] * dslot * es; };
     void *lp[2] = {lam_pos0, lam_pos1}, *ln[2] = {lam_neg0, lam_neg1};
-    int cur = (int)(lam_parity & 1);  // holds lambda_{s+1}
-    for (int64_t s = n_steps - 1; s >= 0; --s) {
-        const int64_t m = track_offsets[s + 1] - track_offsets[s];
-        rc = launch_adjoint(g, P + s * state_stride * es, N + s * state_stride * es, m > 0 ? D + s * dslot * es : nullptr,
-                            lp[cur], ln[cur], lp[cur ^ 1], ln[cur ^ 1], grad_rows + 5 * s, workspace, st);
-        if (rc) return rc;
-        cur ^= 1;
+    int cur = 0;  // lambda_{n_steps} = 0 in buffer 0
+    const int64_t n_seg = (n_steps + ckpt_every - 1) / ckpt_every;
+    for (int64_t c = n_seg - 1; c >= 0; --c) {
+        const int64_t s0 = c * ckpt_every, s1 = (s0 + ckpt_every < n_steps) ? s0 + ckpt_every : n_steps;
+        const int64_t L = s1 - s0;
+        cudaError_t e = cudaMemcpyAsync(SP, static_cast<const char *>(ckpt_pos) + c * state_stride * es,
+                                        (size_t)(field * es), cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(SN, static_cast<const char *>(ckpt_neg) + c * state_stride * es, (size_t)(field * es),
+                                cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return set_cuda_error("cudaMemcpyAsync(checkpoint)", e);
+        // recompute states s0 .. s1-1 of the segment (state j at slot j - s0)
+        for (int64_t j = 0; j + 1 < L; ++j) {
+            rc = launch_step(g, SP + j * state_stride * es, SN + j * state_stride * es, SP + (j + 1) * state_stride * es,
+                             SN + (j + 1) * state_stride * es, dens_of(s0 + j), nullptr, tally_scratch, workspace, st);
+            if (rc) return rc;
+        }
+        // adjoint steps s1-1 .. s0
+        for (int64_t j = L - 1; j >= 0; --j) {
+            rc = launch_adjoint(g, SP + j * state_stride * es, SN + j * state_stride * es, dens_of(s0 + j), lp[cur],
+                                ln[cur], lp[cur ^ 1], ln[cur ^ 1], grad_rows + 5 * (s0 + j), adj_workspace, st);
+            if (rc) return rc;
+            cur ^= 1;
+        }
     }
     return PIC_OK;
 }
