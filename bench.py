@@ -234,6 +234,49 @@ def run_sweep(args):
     return 0
 
 
+def run_adjoint(args):
+    """A full gradient dk_s/d(alpha, mu+, mu-, D+, D-, V) (checkpointed
+    forward + reverse sweep, checkpoints every 64 steps, float32) against one
+    plain forward solve of the same chamber, both end to end through the
+    package API, on the 10 um, r = 0.02 cm column at 300 V."""
+    import torch
+
+    world, rank = _dist()
+    pkg = _pkg()
+    adj = importlib.import_module(PACKAGE + ".adjoint")
+    cfg = pkg.SimulationConfig(**BEAM, grid_size_um=10.0, sampled_radius_cm=0.02, seed=1)
+    for _ in range(max(1, args.warmup)):
+        pkg.run_simulation_b200(cfg, progress=False, return_fields=False)
+        adj.ks_and_gradient(cfg, checkpoint_every=64)
+    plain, full, parts = [], [], []
+    for _ in range(max(1, args.steps)):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        res = pkg.run_simulation_b200(cfg, progress=False, return_fields=False)
+        torch.cuda.synchronize()
+        plain.append(time.perf_counter() - t)
+        t = time.perf_counter()
+        ks, grad, tm = adj.ks_and_gradient(cfg, checkpoint_every=64)
+        torch.cuda.synchronize()
+        full.append(time.perf_counter() - t)
+        parts.append(tm)
+    p, f = statistics.median(plain), statistics.median(full)
+    if rank == 0:
+        print(json.dumps({
+            "metric": "full adjoint gradient wall time / one plain forward solve", "value": f / p, "unit": "x",
+            "n_gpus": world, "steps": len(full), "warmup": args.warmup, "ms_per_step": None,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"10 um column, r 0.02 cm, {cfg.no_xy}x{cfg.no_xy}x{cfg.no_z_with_buffer}, "
+                                   f"{cfg.total_time_steps} steps, 300 V / 0.2 cm, 8.91 Gy/s, seed 1; "
+                                   "checkpoints every 64 steps", "parameters": list(adj.PARAMS)},
+            "plain_forward_s": p, "adjoint_total_s": f,
+            "adjoint_forward_s": statistics.median(t["forward_s"] for t in parts),
+            "adjoint_backward_s": statistics.median(t["backward_s"] for t in parts),
+            "ks": ks, "ks_plain": res.ks, "dks_dtheta": list(grad),
+        }), flush=True)
+    return 0
+
+
 def run_gb300(args):
     import torch
     import torch.distributed as dist
@@ -379,7 +422,7 @@ def main():
     ap.add_argument("--steps", type=int, default=600)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["saturation_sweep"], default="full_electrode_5um")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["saturation_sweep", "adjoint"], default="full_electrode_5um")
     ap.add_argument("--dtype", choices=["float32", "float64"], default="float32")
     ap.add_argument("--e2e-steps", type=int, default=600)
     ap.add_argument("--ref-steps", type=int, default=3)
@@ -398,6 +441,8 @@ def main():
         return run_reference(args)
     if args.workload == "saturation_sweep":
         return run_sweep(args)
+    if args.workload == "adjoint":
+        return run_adjoint(args)
     return run_gb300(args)
 
 

@@ -244,19 +244,32 @@ int pic_adjoint_forward(const pic_grid *g, void *pos0, void *neg0, void *pos1, v
  * pic_adjoint_backward -- the reverse sweep: for each checkpoint segment from
  * the last, recompute the segment's states from its checkpoint into
  * states_pos/neg (ckpt_every states, state_stride apart; kept densities, no
- * deposition; tallies to the 4-double tally_scratch), then run the adjoint
+ * deposition, no tallies), then run the adjoint
  * steps over them backwards. lambda starts at zero in buffer 0 of
  * (lam_*0, lam_*1) (both zeroed by the caller); lambda_0 ends in buffer
- * n_steps & 1. grad_rows[5*s .. 5*s+4] receives step s's
- * dR/d(s+, c+, s-, c-, alpha_dt) (as pic_adjoint_step). Workspaces: the
+ * n_steps & 1. grad[0..4] receives dR/d(s+, c+, s-, c-, alpha_dt) summed
+ * over all steps (each step's terms as pic_adjoint_step's). Workspaces: the
  * step's (pic_step_workspace_bytes) and the adjoint's
  * (pic_adjoint_workspace_bytes), each zeroed once.
  */
 int pic_adjoint_backward(const pic_grid *g, const void *ckpt_pos, const void *ckpt_neg, int64_t state_stride,
                          int64_t n_steps, int64_t ckpt_every, const int64_t *track_offsets, const void *dens_keep,
                          void *states_pos, void *states_neg, void *lam_pos0, void *lam_neg0, void *lam_pos1,
-                         void *lam_neg1, double *grad_rows, double *tally_scratch, void *workspace,
+                         void *lam_neg1, double *grad, void *workspace,
                          int64_t workspace_bytes, void *adj_workspace, int64_t adj_workspace_bytes, uintptr_t stream);
+
+/*
+ * pic_capture_begin / pic_capture_end -- record every launch the library
+ * issues on `stream` between the two calls (made from this host thread) into
+ * a CUDA graph, instantiated and returned in *graph_out (replay with
+ * pic_graph_launch, free with pic_graph_destroy). `stream` must be a stream
+ * the caller created, not the default stream. Nothing runs while capturing:
+ * host-side checks still happen, device work only at replay. Used to replay a
+ * whole adjoint pass (pic_adjoint_forward / _backward) as one graph. No
+ * counterpart in the reference.
+ */
+int pic_capture_begin(uintptr_t stream);
+int pic_capture_end(uintptr_t stream, uintptr_t *graph_out);
 
 /*
  * pic_run_segment -- n_steps consecutive time steps on the device.

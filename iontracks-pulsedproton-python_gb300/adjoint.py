@@ -26,8 +26,9 @@ Method (reverse mode with checkpoints):
 2. backward (``pic_adjoint_backward``), one segment of ``checkpoint_every``
    steps at a time from the last: recompute the segment's states from its
    checkpoint with the kept densities, then run the adjoint steps backwards
-   over them, carrying ``lambda = dR/du`` across segments and recording each
-   step's ``dR/ds+, dR/dc+, dR/ds-, dR/dc-, dR/da``;
+   over them, carrying ``lambda = dR/du`` across segments and summing
+   ``dR/ds+, dR/dc+, dR/ds-, dR/dc-, dR/da`` over the steps (per block on
+   the device, one final reduction);
 3. the chain rule to the six parameters, in float64 on the host.
 
 ``dk_s/dtheta = k_s^2 / I * dR/dtheta``.
@@ -91,7 +92,8 @@ class AdjointRun:
     tracks).
     """
 
-    def __init__(self, config, theta=None, checkpoint_every: int = 64, dtype: str = "float32", rng=None):
+    def __init__(self, config, theta=None, checkpoint_every: int = 64, dtype: str = "float32", rng=None,
+                 use_graphs: bool = False):
         import torch
 
         if dtype not in ("float32", "float64"):
@@ -105,11 +107,43 @@ class AdjointRun:
             raise ValueError("theta must hold (alpha, mu+, mu-, D+, D-, V)")
         self.K = int(checkpoint_every)
         self.dtype = dtype
+        self.use_graphs = bool(use_graphs)
         self.rng = rng if rng is not None else np.random.default_rng(config.seed)
         self.lib = N.load()
         self._eng = None
         self.ks = None
         self.timings = {}
+
+    def _issue(self, launch) -> None:
+        """Run ``launch(stream)`` -- one whole-pass library call -- on the
+        device: captured into a CUDA graph on a private stream and replayed
+        once (one submission for thousands of small launches), or launched
+        directly on the current stream."""
+        torch = self.torch
+        dev = self._eng.device
+        cur = torch.cuda.current_stream(dev)
+        if not self.use_graphs:
+            launch(cur.cuda_stream)
+            return
+        lib = self.lib
+        side = torch.cuda.Stream(device=dev)
+        side.wait_stream(cur)
+        N.check(lib.pic_capture_begin(side.cuda_stream), "pic_capture_begin")
+        h = ctypes.c_void_p()
+        try:
+            launch(side.cuda_stream)
+        except Exception:
+            lib.pic_capture_end(side.cuda_stream, ctypes.byref(h))
+            if h.value:
+                lib.pic_graph_destroy(h)
+            raise
+        N.check(lib.pic_capture_end(side.cuda_stream, ctypes.byref(h)), "pic_capture_end")
+        try:
+            N.check(lib.pic_graph_launch(h, side.cuda_stream), "pic_graph_launch")
+            side.synchronize()
+        finally:
+            lib.pic_graph_destroy(h)
+        cur.wait_stream(side)
 
     # ---- forward ---------------------------------------------------------
     def forward(self) -> float:
@@ -147,14 +181,13 @@ class AdjointRun:
                               f"(raise checkpoint_every to trade memory for recomputation)")
         self.ckpt = torch.empty((2, max(self.n_seg, 1), field), dtype=tdt, device=dev)
         self.dens_keep = torch.empty((max(n_dep, 1), self.dslot), dtype=tdt, device=dev)
-        st = torch.cuda.current_stream(dev).cuda_stream
         off = np.ascontiguousarray(self.offsets)
-        N.check(self.lib.pic_adjoint_forward(
+        self._issue(lambda st: N.check(self.lib.pic_adjoint_forward(
             ctypes.byref(g), eng.pos[0].data_ptr(), eng.neg[0].data_ptr(), eng.pos[1].data_ptr(),
             eng.neg[1].data_ptr(), total, eng.xs.data_ptr(), eng.ys.data_ptr(), off.ctypes.data_as(ctypes.c_void_p),
             self.dens_keep.data_ptr(), eng.counts.data_ptr(), eng.tally.data_ptr(), self.ckpt[0].data_ptr(),
             self.ckpt[1].data_ptr(), self.K, field, eng.workspace.data_ptr(), eng.workspace.numel(), st),
-            "pic_adjoint_forward")
+            "pic_adjoint_forward"))
         tallies = eng.tallies(total)
         eng.check_status()
         # running float64 totals, as the solver and the reference form them
@@ -179,23 +212,21 @@ class AdjointRun:
         dev, tdt = eng.device, eng.pos[0].dtype
         states = torch.empty((2, K, field), dtype=tdt, device=dev)
         lam = torch.zeros((2, 2, field), dtype=tdt, device=dev)  # [buffer][species]
-        grad_rows = torch.zeros((max(total, 1), 5), dtype=torch.float64, device=dev)
-        scratch = torch.zeros(4, dtype=torch.float64, device=dev)
+        grad = torch.zeros(5, dtype=torch.float64, device=dev)
         awb = ctypes.c_int64()
         N.check(lib.pic_adjoint_workspace_bytes(ctypes.byref(g), ctypes.byref(awb)), "pic_adjoint_workspace_bytes")
         adj_ws = torch.zeros(int(awb.value), dtype=torch.uint8, device=dev)
-        st = torch.cuda.current_stream(dev).cuda_stream
         off = np.ascontiguousarray(self.offsets)
-        N.check(lib.pic_adjoint_backward(
+        self._issue(lambda st: N.check(lib.pic_adjoint_backward(
             ctypes.byref(g), self.ckpt[0].data_ptr(), self.ckpt[1].data_ptr(), field, total, K,
             off.ctypes.data_as(ctypes.c_void_p), self.dens_keep.data_ptr(), states[0].data_ptr(),
             states[1].data_ptr(), lam[0, 0].data_ptr(), lam[0, 1].data_ptr(), lam[1, 0].data_ptr(),
-            lam[1, 1].data_ptr(), grad_rows.data_ptr(), scratch.data_ptr(), eng.workspace.data_ptr(),
-            eng.workspace.numel(), adj_ws.data_ptr(), adj_ws.numel(), st), "pic_adjoint_backward")
-        rows = grad_rows[:total].cpu().numpy()
+            lam[1, 1].data_ptr(), grad.data_ptr(), eng.workspace.data_ptr(),
+            eng.workspace.numel(), adj_ws.data_ptr(), adj_ws.numel(), st), "pic_adjoint_backward"))
+        out = grad.cpu().numpy()
         eng.check_status()
         self.timings["backward_s"] = perf_counter() - t0
-        return rows.sum(axis=0)
+        return out
 
     def backward(self) -> np.ndarray:
         """dk_s/dtheta for theta = (alpha, mu+, mu-, D+, D-, V), float64."""
@@ -227,9 +258,10 @@ class AdjointRun:
         self.dens_keep = None
 
 
-def ks_and_gradient(config, theta=None, checkpoint_every: int = 64, dtype: str = "float32", rng=None):
+def ks_and_gradient(config, theta=None, checkpoint_every: int = 64, dtype: str = "float32", rng=None,
+                    use_graphs: bool = False):
     """``(k_s, dk_s/dtheta, timings)`` for theta = (alpha, mu+, mu-, D+, D-, V)."""
-    run = AdjointRun(config, theta, checkpoint_every, dtype, rng)
+    run = AdjointRun(config, theta, checkpoint_every, dtype, rng, use_graphs)
     try:
         ks = run.forward()
         grad = run.backward()

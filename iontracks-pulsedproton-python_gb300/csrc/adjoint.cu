@@ -56,6 +56,7 @@ struct AdjArgs {
     double *grad;         // [kAdjGrad] of this step
     double *partials;     // [blocks][kAdjGrad] 8-byte slots
     unsigned int *counter;
+    int accumulate;       // 1: add the block's sums into its slots (no per-step total)
     int64_t n, kp, c4, items, dp;
     int nzb, nze, gap_end, reflecting;
     T p_lat, p_zm, p_zp, p_cen, n_lat, n_zm, n_zp, n_cen, a, gfac;
@@ -84,6 +85,14 @@ __device__ __forceinline__ void adj_load_add(DF &acc, const double *slot) {
 }
 __device__ __forceinline__ double adj_value(double v) { return v; }
 __device__ __forceinline__ double adj_value(DF v) { return df_value(v); }
+// slot += v, by the one thread that owns the slot
+__device__ __forceinline__ void adj_accumulate(double *slot, double v) { *slot += v; }
+__device__ __forceinline__ void adj_accumulate(double *slot, DF v) {
+    float2 *p = reinterpret_cast<float2 *>(slot);
+    const float2 o = *p;
+    const DF s = df_add(DF{o.x, o.y}, v);
+    *p = make_float2(s.hi, s.lo);
+}
 
 template <int BLOCK, typename A>
 __device__ __forceinline__ void block_sum_n(A (&v)[kAdjGrad], A (*smem)[kAdjGrad]) {
@@ -255,6 +264,15 @@ __global__ void __launch_bounds__(BLOCK) adjoint_step_kernel(AdjArgs<T> a) {
 #pragma unroll
     for (int q = 0; q < kAdjGrad; ++q) v[q] = adj_of(acc[q]);
     block_sum_n<BLOCK>(v, red);
+    if (a.accumulate) {
+        // the backward sweep needs only the sum over steps: each block keeps
+        // its own running sums (same block, same slot, every step; launches
+        // are ordered on the stream), reduced once at the end
+        if (threadIdx.x == 0)
+#pragma unroll
+            for (int q = 0; q < kAdjGrad; ++q) adj_accumulate(a.partials + (int64_t)kAdjGrad * blockIdx.x + q, v[q]);
+        return;
+    }
     if (threadIdx.x == 0) {
 #pragma unroll
         for (int q = 0; q < kAdjGrad; ++q) adj_store(a.partials + (int64_t)kAdjGrad * blockIdx.x + q, v[q]);
@@ -277,6 +295,24 @@ __global__ void __launch_bounds__(BLOCK) adjoint_step_kernel(AdjArgs<T> a) {
         *a.counter = 0u;
         __threadfence();
     }
+}
+
+// Sum of the accumulated block slots of a backward sweep: grad[q] =
+// sum over blocks of slot[b][q], in block order (one block).
+template <typename T, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) adjoint_collect_kernel(const double *slots, int n_blocks, double *grad) {
+    using R = typename AdjRed<T>::type;
+    __shared__ R red[BLOCK / 32][kAdjGrad];
+    R s[kAdjGrad];
+#pragma unroll
+    for (int q = 0; q < kAdjGrad; ++q) s[q] = R{};
+    for (int b = threadIdx.x; b < n_blocks; b += BLOCK)
+#pragma unroll
+        for (int q = 0; q < kAdjGrad; ++q) adj_load_add(s[q], slots + (int64_t)kAdjGrad * b + q);
+    block_sum_n<BLOCK>(s, red);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int q = 0; q < kAdjGrad; ++q) grad[q] = adj_value(s[q]);
 }
 
 // Reflecting wall: the ring's output is a copy of the nearest interior
@@ -337,9 +373,19 @@ int adjoint_workspace_bytes(int64_t *bytes) {
     return PIC_OK;
 }
 
+static int64_t adjoint_blocks(const pic_grid *g) {
+    const int64_t items = g->no_xy * g->no_xy * (g->kpitch / 4);
+    int64_t blocks = (items + 255) / 256;
+    const int64_t cap = step_grid_cap(g->dtype == PIC_F64 ? 1 : 0);
+    if (blocks > cap) blocks = cap;
+    if (blocks > kMaxStepBlocks) blocks = kMaxStepBlocks;
+    return blocks;
+}
+
 template <typename T>
 static int launch_adjoint_t(const pic_grid *g, const void *pos, const void *neg, const void *dens, void *lp_in,
-                            void *ln_in, void *lp_out, void *ln_out, double *grad, void *ws, cudaStream_t st) {
+                            void *ln_in, void *lp_out, void *ln_out, double *grad, void *ws, cudaStream_t st,
+                            bool accumulate) {
     constexpr int BLOCK = 256;
     const int64_t n = g->no_xy, kp = g->kpitch;
     if (g->wall == PIC_WALL_REFLECTING && n >= 3) {
@@ -360,6 +406,7 @@ static int launch_adjoint_t(const pic_grid *g, const void *pos, const void *neg,
     a.lp_out = (T *)lp_out;
     a.ln_out = (T *)ln_out;
     a.grad = grad;
+    a.accumulate = accumulate ? 1 : 0;
     a.counter = reinterpret_cast<unsigned int *>(ws);
     a.partials = reinterpret_cast<double *>(static_cast<char *>(ws) + adj_counter_bytes());
     a.n = n;
@@ -379,10 +426,7 @@ static int launch_adjoint_t(const pic_grid *g, const void *pos, const void *neg,
     a.c_neg = (T)(g->n_zm - g->n_zp);
     int rc = score_test(g, &a.score);
     if (rc) return rc;
-    int64_t blocks = (a.items + BLOCK - 1) / BLOCK;
-    const int64_t cap = step_grid_cap(g->dtype == PIC_F64 ? 1 : 0);
-    if (blocks > cap) blocks = cap;
-    if (blocks > kMaxStepBlocks) blocks = kMaxStepBlocks;
+    const int64_t blocks = adjoint_blocks(g);
     if (flat_index32(n, kp))
         adjoint_step_kernel<T, BLOCK, uint32_t><<<(unsigned)blocks, BLOCK, 0, st>>>(a);
     else
@@ -391,10 +435,26 @@ static int launch_adjoint_t(const pic_grid *g, const void *pos, const void *neg,
 }
 
 int launch_adjoint(const pic_grid *g, const void *pos, const void *neg, const void *dens, void *lp_in, void *ln_in,
-                   void *lp_out, void *ln_out, double *grad, void *ws, cudaStream_t st) {
+                   void *lp_out, void *ln_out, double *grad, void *ws, cudaStream_t st, bool accumulate) {
     if (g->dtype == PIC_F64)
-        return launch_adjoint_t<double>(g, pos, neg, dens, lp_in, ln_in, lp_out, ln_out, grad, ws, st);
-    return launch_adjoint_t<float>(g, pos, neg, dens, lp_in, ln_in, lp_out, ln_out, grad, ws, st);
+        return launch_adjoint_t<double>(g, pos, neg, dens, lp_in, ln_in, lp_out, ln_out, grad, ws, st, accumulate);
+    return launch_adjoint_t<float>(g, pos, neg, dens, lp_in, ln_in, lp_out, ln_out, grad, ws, st, accumulate);
+}
+
+int adjoint_accumulate_begin(const pic_grid *g, void *ws, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(static_cast<char *>(ws) + adj_counter_bytes(), 0,
+                                    (size_t)(adjoint_blocks(g) * kAdjGrad * 8), st);
+    return e == cudaSuccess ? PIC_OK : set_cuda_error("cudaMemsetAsync(adjoint slots)", e);
+}
+
+int adjoint_accumulate_end(const pic_grid *g, void *ws, double *grad, cudaStream_t st) {
+    const double *slots = reinterpret_cast<const double *>(static_cast<char *>(ws) + adj_counter_bytes());
+    const int nb = (int)adjoint_blocks(g);
+    if (g->dtype == PIC_F64)
+        adjoint_collect_kernel<double, 256><<<1, 256, 0, st>>>(slots, nb, grad);
+    else
+        adjoint_collect_kernel<float, 256><<<1, 256, 0, st>>>(slots, nb, grad);
+    return check_launch("adjoint_collect_kernel");
 }
 
 }  // namespace pic

@@ -433,7 +433,7 @@ int pic_adjoint_forward(const pic_grid *g, void *pos0, void *neg0, void *pos1, v
 int pic_adjoint_backward(const pic_grid *g, const void *ckpt_pos, const void *ckpt_neg, int64_t state_stride,
                          int64_t n_steps, int64_t ckpt_every, const int64_t *track_offsets, const void *dens_keep,
                          void *states_pos, void *states_neg, void *lam_pos0, void *lam_neg0, void *lam_pos1,
-                         void *lam_neg1, double *grad_rows, double *tally_scratch, void *workspace,
+                         void *lam_neg1, double *grad, void *workspace,
                          int64_t workspace_bytes, void *adj_workspace, int64_t adj_workspace_bytes, uintptr_t stream) {
     int rc = check_grid(g);
     if (rc) return rc;
@@ -441,7 +441,7 @@ int pic_adjoint_backward(const pic_grid *g, const void *ckpt_pos, const void *ck
         (rc = check_fields(lam_pos0, lam_neg0, lam_pos1, lam_neg1)))
         return rc;
     if (n_steps < 0 || ckpt_every < 1) return set_error(PIC_E_INVALID, "n_steps must be >= 0 and ckpt_every >= 1");
-    if (!track_offsets || !grad_rows || !tally_scratch) return set_error(PIC_E_INVALID, "null pointer argument");
+    if (!track_offsets || !grad) return set_error(PIC_E_INVALID, "null pointer argument");
     const int64_t field = g->no_xy * g->no_xy * g->kpitch;
     if (state_stride < field || state_stride % 8 != 0)
         return set_error(PIC_E_INVALID, "state_stride must be >= no_xy^2 * kpitch and a multiple of 8 elements");
@@ -469,6 +469,7 @@ int pic_adjoint_backward(const pic_grid *g, const void *ckpt_pos, const void *ck
     void *lp[2] = {lam_pos0, lam_pos1}, *ln[2] = {lam_neg0, lam_neg1};
     int cur = 0;  // lambda_{n_steps} = 0 in buffer 0
     const int64_t n_seg = (n_steps + ckpt_every - 1) / ckpt_every;
+    if ((rc = adjoint_accumulate_begin(g, adj_workspace, st))) return rc;
     for (int64_t c = n_seg - 1; c >= 0; --c) {
         const int64_t s0 = c * ckpt_every, s1 = (s0 + ckpt_every < n_steps) ? s0 + ckpt_every : n_steps;
         const int64_t L = s1 - s0;
@@ -481,18 +482,18 @@ int pic_adjoint_backward(const pic_grid *g, const void *ckpt_pos, const void *ck
         // recompute states s0 .. s1-1 of the segment (state j at slot j - s0)
         for (int64_t j = 0; j + 1 < L; ++j) {
             rc = launch_step(g, SP + j * state_stride * es, SN + j * state_stride * es, SP + (j + 1) * state_stride * es,
-                             SN + (j + 1) * state_stride * es, dens_of(s0 + j), nullptr, tally_scratch, workspace, st);
+                             SN + (j + 1) * state_stride * es, dens_of(s0 + j), nullptr, nullptr, workspace, st);
             if (rc) return rc;
         }
         // adjoint steps s1-1 .. s0
         for (int64_t j = L - 1; j >= 0; --j) {
             rc = launch_adjoint(g, SP + j * state_stride * es, SN + j * state_stride * es, dens_of(s0 + j), lp[cur],
-                                ln[cur], lp[cur ^ 1], ln[cur ^ 1], grad_rows + 5 * (s0 + j), adj_workspace, st);
+                                ln[cur], lp[cur ^ 1], ln[cur ^ 1], nullptr, adj_workspace, st, true);
             if (rc) return rc;
             cur ^= 1;
         }
     }
-    return PIC_OK;
+    return adjoint_accumulate_end(g, adj_workspace, grad, st);
 }
 
 int pic_run_segment(const pic_grid *g, void *pos0, void *neg0, void *pos1, void *neg1, int64_t parity,
@@ -537,6 +538,31 @@ int pic_graph_create(const pic_grid *g, void *pos0, void *neg0, void *pos1, void
         return rc;
     }
     if (e != cudaSuccess) return set_cuda_error("cudaStreamEndCapture", e);
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return set_cuda_error("cudaGraphInstantiate", e);
+    *graph_out = reinterpret_cast<uintptr_t>(exec);
+    return PIC_OK;
+}
+
+int pic_capture_begin(uintptr_t stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (st == nullptr || st == cudaStreamLegacy || st == cudaStreamPerThread)
+        return set_error(PIC_E_INVALID, "capture needs a stream created by the caller (not the default stream)");
+    cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    return e == cudaSuccess ? PIC_OK : set_cuda_error("cudaStreamBeginCapture", e);
+}
+
+int pic_capture_end(uintptr_t stream, uintptr_t *graph_out) {
+    if (!graph_out) return set_error(PIC_E_INVALID, "graph_out is null");
+    *graph_out = 0;
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(reinterpret_cast<cudaStream_t>(stream), &graph);
+    if (e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return set_cuda_error("cudaStreamEndCapture", e);
+    }
     cudaGraphExec_t exec = nullptr;
     e = cudaGraphInstantiate(&exec, graph, 0);
     cudaGraphDestroy(graph);

@@ -98,7 +98,9 @@ int step_noalloc(const pic_grid *g, const void *pos_in, const void *neg_in, void
 
 int adjoint_workspace_bytes(int64_t *bytes);
 int launch_adjoint(const pic_grid *g, const void *pos, const void *neg, const void *dens, void *lp_in, void *ln_in,
-                   void *lp_out, void *ln_out, double *grad, void *ws, cudaStream_t st);
+                   void *lp_out, void *ln_out, double *grad, void *ws, cudaStream_t st, bool accumulate = false);
+int adjoint_accumulate_begin(const pic_grid *g, void *ws, cudaStream_t st);
+int adjoint_accumulate_end(const pic_grid *g, void *ws, double *grad, cudaStream_t st);
 
 int sample_disc(const double *u, int64_t n_pairs, double scale, double mid, double radius_sq, int64_t n_wanted,
                 double *xs, double *ys, int64_t *n_accepted, int64_t *n_pairs_used);

@@ -35,6 +35,7 @@ __global__ void __launch_bounds__(BLOCK) step_kernel(StepArgs<T> a) {
     const I stride = (I)gridDim.x * BLOCK, items = (I)a.items;
     for (I item = (I)blockIdx.x * BLOCK + threadIdx.x; item < items; item += stride)
         flat_item<T, I>(a, item, t_rec, t_p, t_n, t_inj);
+    if (!a.tally) return;  // no tallies wanted (a recomputation): no reduction
     if constexpr (sizeof(T) == 4) {
         DF v[4] = {df_of(t_inj), df_of(t_rec), df_of(t_p), df_of(t_n)};
         finish_tally_df<BLOCK>(v, a.partials, a.counter, a.tally, a.injected_scale);

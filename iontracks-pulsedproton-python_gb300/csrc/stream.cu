@@ -455,6 +455,7 @@ __global__ void __launch_bounds__(stream_max_threads(IPT), 1) stream_step_kernel
             g += nplanes;
         }
     }
+    if (!a.tally) return;  // no tallies wanted (a recomputation): no reduction
     double v[4] = {t_inj.value(), t_rec.value(), t_p.value(), t_n.value()};
     finish_tally_rt(v, a.partials, a.counter, a.tally, a.injected_scale);
 }

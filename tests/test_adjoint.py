@@ -134,3 +134,19 @@ def test_checkpoint_spacing_does_not_change_the_gradient():
     g = [A.ks_and_gradient(cfg, None, checkpoint_every=k, dtype="float64")[1] for k in (1, 3, 1000)]
     np.testing.assert_allclose(g[0], g[1], rtol=1e-10)
     np.testing.assert_allclose(g[0], g[2], rtol=1e-10)
+
+
+@pytest.mark.gpu
+def test_fit_alpha_to_a_saturation_curve(oracle):
+    """Fit alpha to a synthetic k_s(V) curve: the 10 um, r = 0.02 cm column
+    at 8 voltages over 50-400 V, targets from the float64 oracle at alpha
+    scaled by 1.3; gradient steps from the float32 adjoint recover it."""
+    A = _adj()
+    alpha0 = pkg().RECOMBINATION_ALPHA_CM3_S
+    volts = np.linspace(50.0, 400.0, 8)
+    cfgs = [make_config("column_10um_r02", voltage_V=float(v)) for v in volts]
+    target = [oracle.run(c, mode="batched", alpha_cm3_s=1.3 * alpha0, threads=16, keep_fields=False)["ks"]
+              for c in cfgs]
+    alpha, history = A.fit_alpha(cfgs, target, alpha0, iterations=6)
+    assert alpha == pytest.approx(1.3 * alpha0, rel=1e-4)
+    assert history[-1][1] < 1e-6 * history[0][1]
