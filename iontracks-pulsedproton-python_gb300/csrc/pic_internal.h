@@ -39,7 +39,7 @@ __host__ __device__ constexpr int stream_max_threads(int ipt) {
 }
 constexpr int kStreamMaxSmem = 227 * 1024;
 // AUTO picks the streaming kernel from this many allocated cells (no_xy^2 * kpitch)
-constexpr int64_t kStreamMinCells = 6000000;
+constexpr int64_t kStreamMinCells = 200000000;
 
 // Launch shape of the streaming step kernel.
 struct StreamShape {

@@ -122,10 +122,12 @@ def test_launch_shape_resolution_without_a_gpu():
     assert s["planes_per_item"] == 64  # 1066 x 152 tiles: > 12 items per SM even at 64 planes
     small = eng.make_grid(make_config("column_10um_r008"))
     assert eng.resolve_shape(small)["variant"] == "flat"
-    # 208 x 208 x 408 = 17.7 M cells: streaming, with few planes per item so
-    # that 30 j-tiles still give every SM work
+    # 208 x 208 x 408 = 17.7 M cells: flat by default (faster below ~2e8
+    # cells); streaming when asked, with few planes per item so that 30
+    # j-tiles still give every SM work
     mid = eng.make_grid(make_config("column_5um_r05_d8p91"))
-    s = eng.resolve_shape(mid)
+    assert eng.resolve_shape(mid)["variant"] == "flat"
+    s = eng.resolve_shape(eng.make_grid(make_config("column_5um_r05_d8p91"), shape={"variant": "stream"}))
     assert s["variant"] == "stream" and 4 <= s["planes_per_item"] <= 8
     f64 = eng.make_grid(make_config("full_electrode_5um_10p"), dtype="float64")
     assert eng.resolve_shape(f64)["variant"] == "flat"
