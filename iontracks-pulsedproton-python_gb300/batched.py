@@ -30,7 +30,21 @@ from .engine import make_grid
 from .pulses import TrackSampler, build_track_schedule
 from .state import Diagnostics, collection_efficiency
 
-ITEMS_PER_BLOCK = 256 * 8
+# The batched step runs 3 resident 256-thread blocks per SM (80 registers).
+# Items per block are chosen per phase for about four blocks per resident slot:
+# few, long blocks amortise each block's set-up and reduction on the big
+# phases; enough blocks keep every SM busy when few small grids remain.
+BLOCKS_PER_SM = 3
+WAVES = 4
+MIN_ITEMS_PER_BLOCK = 256
+MAX_ITEMS_PER_BLOCK = 1 << 16
+
+
+def items_per_block(total_items: int, sms: int) -> int:
+    """Work items per block for a phase of ``total_items`` items."""
+    want = -(-int(total_items) // (WAVES * BLOCKS_PER_SM * max(1, sms)))
+    want = -(-want // 256) * 256
+    return max(MIN_ITEMS_PER_BLOCK, min(MAX_ITEMS_PER_BLOCK, want))
 
 
 class PicBatchCfg(ctypes.Structure):
@@ -137,7 +151,7 @@ def run_batched_b200(
     if not torch.cuda.is_available():
         raise RuntimeError("run_batched_b200 needs a CUDA device (a GB300); none is visible")
     lib = N.load()
-    N.device_info()
+    sms = N.device_info()[0]
     dev = torch.device("cuda", torch.cuda.current_device())
     n_cfg = len(configs)
     if n_cfg == 0:
@@ -201,51 +215,52 @@ def run_batched_b200(
     xs_dev = torch.from_numpy(np.concatenate(xs_parts) if base else np.zeros(1)).to(dev)
     ys_dev = torch.from_numpy(np.concatenate(ys_parts) if base else np.zeros(1)).to(dev)
 
-    # --- per global step: tasks (grid, first track, first warp)
+    # --- per global step: tasks (grid, first track, first warp), in grid
+    # order within a step; M[s, c] = tracks of grid c at global step s
     S = max(totals)
-    t_cfg, t_first, t_prefix = [], [], []
+    M = np.zeros((S, n_cfg), dtype=np.int64)
+    F = np.zeros((S, n_cfg), dtype=np.int64)  # first track of (s, c) in the packed arrays
+    for c in range(n_cfg):
+        M[: totals[c], c] = np.diff(offsets[c])
+        F[: totals[c], c] = track_base[c] + offsets[c][:-1]
+    s_idx, c_idx = np.nonzero(M)  # row-major: by step, then grid
+    vals = M[s_idx, c_idx]
     step_task_off = np.zeros(S + 1, dtype=np.int64)
-    step_tracks = np.zeros(S, dtype=np.int64)
-    counts_by_cfg = [np.diff(o) for o in offsets]
-    for s in range(S):
-        w = 0
-        for c in range(n_cfg):
-            if s < totals[c]:
-                m = int(counts_by_cfg[c][s])
-                if m > 0:
-                    t_cfg.append(c)
-                    t_first.append(track_base[c] + int(offsets[c][s]))
-                    t_prefix.append(w)
-                    w += m
-        step_tracks[s] = w
-        step_task_off[s + 1] = len(t_cfg)
-    task_cfg = torch.tensor(t_cfg if t_cfg else [0], dtype=torch.int32, device=dev)
-    task_first = torch.tensor(t_first if t_first else [0], dtype=torch.int64, device=dev)
-    task_prefix = torch.tensor(t_prefix if t_prefix else [0], dtype=torch.int64, device=dev)
+    np.cumsum(np.bincount(s_idx, minlength=S), out=step_task_off[1:])
+    step_tracks = M.sum(axis=1)
+    excl = np.cumsum(vals) - vals  # warps before each task, over all steps
+    t_prefix = excl - excl[step_task_off[s_idx]] if len(vals) else excl
+    t_cfg, t_first = c_idx.astype(np.int32), F[s_idx, c_idx]
+    one = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a if len(a) else np.zeros(1), dtype=dt)).to(dev)
+    task_cfg = one(t_cfg, np.int32)
+    task_first = one(t_first, np.int64)
+    task_prefix = one(t_prefix, np.int64)
 
     # --- work tables, one per set of active grids
     phases = []
     max_blocks = 1
+    items_a = np.asarray(items, dtype=np.int64)
     for s0, s1, active in _phases(totals):
-        blk_cfg, i0, i1 = [], [], []
+        act = np.asarray(active, dtype=np.int64)
+        ipb = items_per_block(int(items_a[act].sum()), sms)
+        nb = np.maximum(1, -(-items_a[act] // ipb))
+        first = np.concatenate([[0], np.cumsum(nb)[:-1]])
         cfg_blk0 = np.zeros(n_cfg, dtype=np.int32)
         cfg_nblk = np.zeros(n_cfg, dtype=np.int32)
-        for c in active:
-            nb = max(1, -(-items[c] // ITEMS_PER_BLOCK))
-            cfg_blk0[c] = len(blk_cfg)
-            cfg_nblk[c] = nb
-            for b in range(nb):
-                blk_cfg.append(c)
-                i0.append(b * items[c] // nb)
-                i1.append((b + 1) * items[c] // nb)
+        cfg_blk0[act] = first
+        cfg_nblk[act] = nb
+        blk_cfg = np.repeat(act, nb)
+        b = np.arange(int(nb.sum()), dtype=np.int64) - np.repeat(first, nb)  # block index within its grid
+        it, nbr = items_a[blk_cfg], np.repeat(nb, nb)
+        i0, i1 = b * it // nbr, (b + 1) * it // nbr
         max_blocks = max(max_blocks, len(blk_cfg))
         phases.append((s0, s1, dict(
-            blk_cfg=torch.tensor(blk_cfg, dtype=torch.int32, device=dev),
-            blk_item0=torch.tensor(i0, dtype=torch.int64, device=dev),
-            blk_item1=torch.tensor(i1, dtype=torch.int64, device=dev),
+            blk_cfg=torch.from_numpy(blk_cfg.astype(np.int32)).to(dev),
+            blk_item0=torch.from_numpy(i0).to(dev),
+            blk_item1=torch.from_numpy(i1).to(dev),
             cfg_blk0=torch.from_numpy(cfg_blk0).to(dev),
             cfg_nblk=torch.from_numpy(cfg_nblk).to(dev),
-            n_blocks=len(blk_cfg),
+            n_blocks=int(len(blk_cfg)),
         )))
     # 32-bit offsets when every grid's fields are < 2^31 elements
     index32 = all(int(g.no_xy) <= 16383 and int(g.no_xy) ** 2 * int(g.kpitch) < 2**31 for g in grids)
