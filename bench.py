@@ -203,7 +203,7 @@ def run_sweep(args):
 
     world, rank = _dist()
     pkg = _pkg()
-    cfgs = pkg.saturation_sweep_configs()
+    cfgs = pkg.saturation_sweep_configs()[: max(1, args.sweep_configs)]
     vox = sum(_interior(c) * int(c.total_time_steps) for c in cfgs)
     # warm-up: load the kernels, pay first-use costs outside the timing
     pkg.run_batched_b200(cfgs[:2])
@@ -224,9 +224,9 @@ def run_sweep(args):
             "unit": "voxel-steps/s", "n_gpus": world, "steps": int(max(c.total_time_steps for c in cfgs)),
             "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "saturation sweep: 64 configs, 25-400 V log-spaced, gaps 0.1/0.2/0.3 cm, "
-                                   "1-100 Gy/s, 100-1000 us pulses, 5/10 um voxels, r 0.008-0.03 cm, seeds 1-64",
-                       "interior_voxel_steps": vox},
+            "config": {"workload": f"saturation sweep: {len(cfgs)} of 64 configs, 25-400 V log-spaced, gaps "
+                                   "0.1/0.2/0.3 cm, 1-100 Gy/s, 100-1000 us pulses, 5/10 um voxels, "
+                                   "r 0.008-0.03 cm, seeds 1-64", "interior_voxel_steps": vox},
             "batched_s": t_batch, "sequential_plain_s": t_plain, "speedup_vs_sequential": t_plain / t_batch,
             "max_abs_dks_batched_vs_plain": dks,
         }
@@ -427,6 +427,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=600)
     ap.add_argument("--ref-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--sweep-configs", dest="sweep_configs", type=int, default=64,
+                    help="saturation_sweep: run the first N of the 64 configurations (profiling-size cases)")
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner")
     ap.add_argument("--variant", choices=["auto", "flat", "stream"], default="auto")
     ap.add_argument("--tile-rows", dest="tile_rows", type=int, default=0)
