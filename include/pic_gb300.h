@@ -14,9 +14,10 @@
  * k fastest, kpitch = pic_kpitch(nzb) >= nzb (rows start 32-byte aligned).
  * Elements k >= nzb - 1 and k == 0 are the z end planes plus padding and are
  * kept at zero. Fields are float32 (PIC_F32) or float64 (PIC_F64, the
- * validation build); the 2D density follows the field type and is laid out
- * dens[i][j], 0 <= j < pic_dens_pitch(no_xy) (rows padded to 4 elements so
- * each starts 16-byte aligned). Per-step tallies
+ * validation build). A step's deposition follows the field type and is laid
+ * out as pairs dens[i][j] = {G * density, G * (sum of the density of the four
+ * lateral neighbours)}, 0 <= j < pic_dens_pitch(no_xy) (rows padded to 4
+ * pairs so each starts 32-byte aligned; G = gaussian_factor). Per-step tallies
  * are always float64: tally[s] = {injected, recombined, sum n+, sum n-} over
  * the scored voxels.
  */
@@ -88,7 +89,7 @@ int pic_abi_version(void);
 /* k pitch for a given no_z_with_buffer: nzb rounded up to 8 elements. */
 int64_t pic_kpitch(int64_t nzb);
 
-/* Row pitch of the 2D density: no_xy rounded up to 4 elements. */
+/* Row pitch of the deposition pairs: no_xy rounded up to 4 pairs. */
 int64_t pic_dens_pitch(int64_t no_xy);
 
 /* Checks that a CUDA device of compute capability 10.3 is current; fills the
@@ -111,13 +112,15 @@ int pic_workspace_status(void *workspace, int32_t reset, uintptr_t stream, int32
 int pic_resolve_shape(const pic_grid *g, pic_grid *resolved);
 
 /*
- * pic_deposit -- sum one step's track Gaussians into the 2D density.
+ * pic_deposit -- sum one step's track Gaussians into the deposition pairs.
  *
- * dens[i][j] += sum_t exp(-(i-x_t)^2 h2/b2) exp(-(j-y_t)^2 h2/b2) over each
- * track's truncated stencil box [ceil(x-cut), floor(x+cut)] clipped to the
- * grid (dimensionless; the gaussian factor is applied by pic_step), and
- * counts[int(x)][int(y)] += 1 per track. dens must be zero on entry for a
- * fresh step (pic_step zeroes the next step's buffer).
+ * With g_i = exp(-(i-x_t)^2 h2/b2) on each track's truncated stencil box
+ * [ceil(x-cut), floor(x+cut)] clipped to the grid (0 outside it), and the
+ * same g_j in y: dens[i][j].x += G sum_t g_i g_j and
+ * dens[i][j].y += G sum_t ((g_{i-1} + g_{i+1}) g_j + g_i (g_{j-1} + g_{j+1})),
+ * i.e. the density and its four lateral neighbours' sum, both times
+ * G = gaussian_factor; counts[int(x)][int(y)] += 1 per track. dens must be
+ * zero on entry for a fresh step (pic_step zeroes the next step's buffer).
  *
  * Replaces: _insert_track_numba's per-track stencil (solver_numba.py:84-98),
  * _precompute_track_gaussians + _build_row_index +
@@ -132,8 +135,9 @@ int pic_deposit(const pic_grid *g, const double *xs, const double *ys, int64_t n
  * pic_step -- one fused time step: deposition broadcast, Lax-Wendroff sweep,
  * recombination sink, lateral wall and the step's tallies.
  *
- * Reads pos_in/neg_in (+ gaussian_factor * dens in every gap layer when dens
- * is non-null), writes every column of pos_out/neg_out: the interior by the
+ * Reads pos_in/neg_in (+ the deposition in every gap layer when dens is
+ * non-null: a column's own density on its values, its neighbours' sum on the
+ * stencil's lateral sum), writes every column of pos_out/neg_out: the interior by the
  * 7-point Lax-Wendroff stencil minus alpha*dt*n+*n-, the outer ring carried
  * with the step's deposition (absorbing) or mirrored from the new interior
  * (reflecting). Writes tally[0..3] = {injected, recombined, sum n+, sum n-}
@@ -162,9 +166,9 @@ int pic_step(const pic_grid *g, const void *pos_in, const void *neg_in, void *po
  * outputs.
  *
  * No counterpart in the reference (whose drivers allocate their own arrays).
- * Limit: the 2D density must fit the 8 MiB static scratch -- no_xy <= 1448
- * for float32 fields, <= 1024 for float64 -- else PIC_E_CAPACITY. Every GPU
- * that loads the library holds the array (8 MiB plus the tally workspace)
+ * Limit: the deposition pairs must fit the 16 MiB static scratch -- no_xy <=
+ * 1448 for float32 fields, <= 1024 for float64 -- else PIC_E_CAPACITY. Every
+ * GPU that loads the library holds the array (16 MiB plus the tally workspace)
  * until exit. All calls share it: calls that overlap on the GPU race, so
  * serialise them. The first call on a device looks up the array's device
  * address; make it before any stream capture.
@@ -208,7 +212,7 @@ int pic_sample_disc_pcg64(uint64_t *state, double scale, double mid, double radi
  * charge, for k_s = I / (I - R).
  *
  * pic_adjoint_step -- one step backwards. Given the state u_s that step s
- * read (pos/neg), its 2D density (dens, or NULL when the step deposited
+ * read (pos/neg), its deposition pairs (dens, or NULL when the step deposited
  * nothing) and lambda_{s+1} = dR/du_{s+1} (lam_*_in), writes
  * lambda_s = dR/du_s (lam_*_out) and grad[0..4] = this step's contribution to
  * dR/ds+, dR/dc+, dR/ds-, dR/dc-, dR/d(alpha_dt), where s = D dt / h^2 and
@@ -230,9 +234,9 @@ int pic_adjoint_step(const pic_grid *g, const void *pos, const void *neg, const 
  * tally[4*s ..], the track histogram into counts. Before step
  * c * ckpt_every it copies the state into checkpoint c
  * (ckpt_pos/neg + c * state_stride elements; state_stride >= no_xy^2 *
- * kpitch, a multiple of 8). Every step with tracks keeps its 2D density: the
+ * kpitch, a multiple of 8). Every step with tracks keeps its deposition: the
  * d-th such step deposits into slot d of dens_keep
- * ([n_dep][no_xy][pic_dens_pitch], cleared here first), which the backward
+ * ([n_dep][no_xy][pic_dens_pitch] pairs, cleared here first), which the backward
  * pass reads instead of depositing again. Workspace as pic_step.
  */
 int pic_adjoint_forward(const pic_grid *g, void *pos0, void *neg0, void *pos1, void *neg1, int64_t n_steps,
@@ -322,7 +326,7 @@ int pic_graph_destroy(uintptr_t graph);
  */
 typedef struct pic_batch_cfg {
     int64_t field_off;  /* element offset of the grid's [no_xy][no_xy][kpitch] fields    */
-    int64_t dens_off;   /* element offset of its [no_xy][dens_pitch] density           */
+    int64_t dens_off;   /* pair offset of its [no_xy][dens_pitch] deposition pairs     */
     int64_t counts_off; /* offset of its [no_xy][no_xy] track histogram                */
     int64_t tally_off;  /* row offset of its [steps][4] tallies                         */
     pic_grid grid;      /* the grid's scalars (dtype must match the batch)             */
@@ -340,7 +344,7 @@ typedef struct pic_batch_launch {
                                            /*  faster decode); 0: 64-bit offsets (any grid)  */
     const int32_t *cfg_blk0, *cfg_nblk;    /* device, per grid: first block, block count     */
     void *pos[2], *neg[2];                 /* device, packed fields of time levels 0 and 1   */
-    void *dens[2];                         /* device, packed densities, by step parity       */
+    void *dens[2];                         /* device, packed deposition pairs, by step parity */
     const double *xs, *ys;                 /* device, packed track centres                   */
     const int32_t *task_cfg;               /* device, per task (grid, tracks of one step):   */
     const int64_t *task_first;             /*   grid, first track, and first warp within the */

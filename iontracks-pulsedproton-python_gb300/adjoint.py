@@ -170,7 +170,7 @@ class AdjointRun:
         self.field = field
         dev, tdt = eng.device, eng.pos[0].dtype
         n = int(g.no_xy)
-        self.dslot = n * ((n + 3) // 4 * 4)
+        self.dslot = 2 * n * ((n + 3) // 4 * 4)  # one step's deposition pairs
         n_dep = int(np.count_nonzero(schedule))
         es = 4 if self.dtype == "float32" else 8
         need = (self.n_seg + self.K) * 2 * field * es + n_dep * self.dslot * es + 4 * field * es

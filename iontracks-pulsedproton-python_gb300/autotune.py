@@ -42,7 +42,7 @@ def candidate_shapes(grid, quick: bool = False) -> list[dict]:
     for tj, cw, ctas, stages, li in itertools.product(tjs, cws, (1, 2), stage_counts, planes):
         if tj > grid.no_xy - 2:
             continue
-        smem = (2 * stages * 8 + 127) // 128 * 128 + stages * (2 * (tj + 2) * kp + ((tj + 8) & ~3)) * 4
+        smem = (2 * stages * 8 + 127) // 128 * 128 + stages * (2 * (tj + 2) * kp + 2 * ((tj + 8) & ~3)) * 4
         if ctas * (smem + 3 * 1024) > _SMEM_PER_SM:
             continue
         ipt = -(-(tj * (kp // 4)) // (cw * 32))

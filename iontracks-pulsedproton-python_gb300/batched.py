@@ -194,7 +194,7 @@ def run_batched_b200(
         co = _align(co + n * n)
         to += t
         items.append(n * n * (kp // 4))
-    need = 4 * fo * es + 2 * do * es + co * 4 + to * 32 + 16 * base
+    need = 4 * fo * es + 4 * do * es + co * 4 + to * 32 + 16 * base
     free, _ = torch.cuda.mem_get_info(dev)
     if need > 0.9 * free:
         raise MemoryError(f"batch needs {need / 2**30:.2f} GiB of device memory, {free / 2**30:.2f} GiB free")
@@ -209,7 +209,7 @@ def run_batched_b200(
     kw = dict(device=dev)
     pos = [torch.zeros(max(fo, 1), dtype=tdt, **kw) for _ in range(2)]
     neg = [torch.zeros(max(fo, 1), dtype=tdt, **kw) for _ in range(2)]
-    dens = [torch.zeros(max(do, 1), dtype=tdt, **kw) for _ in range(2)]
+    dens = [torch.zeros(max(2 * do, 2), dtype=tdt, **kw) for _ in range(2)]  # deposition pairs
     counts = torch.zeros(max(co, 1), dtype=torch.int32, **kw)
     tally = torch.zeros((max(to, 1), 4), dtype=torch.float64, **kw)
     xs_dev = torch.from_numpy(np.concatenate(xs_parts) if base else np.zeros(1)).to(dev)

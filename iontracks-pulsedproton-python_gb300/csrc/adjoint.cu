@@ -50,7 +50,7 @@ constexpr int kAdjGrad = 5;  // dR/ds+, dR/dc+, dR/ds-, dR/dc-, dR/da
 template <typename T>
 struct AdjArgs {
     const T *pos, *neg;   // u_s
-    const T *dens;        // density of step s (null: none)
+    const pair_t<T> *dens;  // deposition pairs of step s (null: none)
     const T *lp, *ln;     // lambda_{s+1}
     T *lp_out, *ln_out;   // lambda_s
     double *grad;         // [kAdjGrad] of this step
@@ -140,7 +140,8 @@ __global__ void __launch_bounds__(BLOCK) adjoint_step_kernel(AdjArgs<T> a) {
         }
         const bool interior = interior_col(i, j, n);
         const bool scored = interior && scored_col_t<I>(a.score, i, j);
-        const T dc = a.dens ? a.gfac * a.dens[i * dp + j] : T(0);
+        const pair_t<T> dpr = a.dens ? a.dens[i * dp + j] : pair_t<T>{T(0), T(0)};
+        const T dc = dpr.x, dl = dpr.y;  // this column's deposition, its neighbours' sum
 
         // mu of this column (zero off the interior and on invalid k), with
         // its k-1 / k+4 neighbours
@@ -224,16 +225,19 @@ __global__ void __launch_bounds__(BLOCK) adjoint_step_kernel(AdjArgs<T> a) {
             for (int e = 0; e < 4; ++e) SP.v[e] = SN.v[e] = T(0);
             const I di = n * kp;
             const I nbo[4] = {off - di, off + di, off - kp, off + kp};
-            const I nbd[4] = {(i - 1) * dp + j, (i + 1) * dp + j, i * dp + j - 1, i * dp + j + 1};
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                const T d = a.dens ? a.gfac * a.dens[nbd[q]] : T(0);
-                const V4<T> A = state4(a.pos, nbo[q], d, g), B = state4(a.neg, nbo[q], d, g);
+                const V4<T> A = load4(a.pos + nbo[q]), B = load4(a.neg + nbo[q]);
 #pragma unroll
                 for (int e = 0; e < 4; ++e) {
                     SP.v[e] += A.v[e];
                     SN.v[e] += B.v[e];
                 }
+            }
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {  // the neighbours' deposition, summed
+                SP.v[e] += g[e] ? dl : T(0);
+                SN.v[e] += g[e] ? dl : T(0);
             }
             T gs[kAdjGrad];
 #pragma unroll
@@ -400,7 +404,7 @@ static int launch_adjoint_t(const pic_grid *g, const void *pos, const void *neg,
     AdjArgs<T> a;
     a.pos = (const T *)pos;
     a.neg = (const T *)neg;
-    a.dens = (const T *)dens;
+    a.dens = (const pair_t<T> *)dens;
     a.lp = (const T *)lp_in;
     a.ln = (const T *)ln_in;
     a.lp_out = (T *)lp_out;

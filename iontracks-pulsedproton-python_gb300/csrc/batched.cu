@@ -1,7 +1,7 @@
 // batched.cu -- many independent chamber configurations advanced together.
 //
 // The grids of a batch live at their own offsets in packed buffers (fields,
-// 2D densities, track histograms, tallies), described by a device table of
+// 2D deposition pairs, track histograms, tallies), described by a device table of
 // pic_batch_cfg entries (each grid's pic_grid scalars and offsets). One global
 // step advances every active grid by one of its own time steps with two
 // launches for the whole batch:
@@ -34,8 +34,8 @@ struct BatchStepArgs {
     const int32_t *cfg_blk0, *cfg_nblk;
     const T *pos_in, *neg_in;
     T *pos_out, *neg_out;
-    const T *dens;    // packed density buffer of this step
-    T *dens_zero;     // packed buffer of the next step, cleared here
+    const pair_t<T> *dens;  // packed deposition pairs of this step
+    pair_t<T> *dens_zero;   // packed pairs of the next step, cleared here
     double *tally;    // packed [rows][4]
     double *partials; // [n_blocks][4]
     unsigned int *counters;  // [n_cfgs]
@@ -67,7 +67,7 @@ __device__ void grid_args(const pic_batch_cfg &C, const BatchStepArgs<T> &b, Ste
     a.score.two_mid = (int64_t)(2.0 * g.mid_xy);
     const double r4 = 4.0 * g.scoring_radius_sq;
     a.score.thr4 = r4 >= 4.0e18 ? (int64_t)4.0e18 : (int64_t)ceil(r4) - 1;
-    a.injected_scale = g.gaussian_factor * (double)g.no_z;
+    a.injected_scale = (double)g.no_z;
 }
 
 // Reduction type of a grid's tallies: double-float for float32 fields (no
@@ -140,7 +140,8 @@ __global__ void __launch_bounds__(WARPS * 32) batched_deposit_kernel(const pic_b
                                                                       const int64_t *task_first,
                                                                       const int64_t *task_prefix, int n_tasks,
                                                                       int64_t total, const double *xs,
-                                                                      const double *ys, T *dens, uint32_t *counts) {
+                                                                      const double *ys, pair_t<T> *dens,
+                                                                      uint32_t *counts) {
     const int64_t w = (int64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
     if (w >= total) return;
     // last task whose first warp is <= w
@@ -153,7 +154,7 @@ __global__ void __launch_bounds__(WARPS * 32) batched_deposit_kernel(const pic_b
     const int64_t idx = task_first[lo] + (w - task_prefix[lo]);
     const int64_t n = C.grid.no_xy;
     deposit_track<T>(xs[idx], ys[idx], n, (n + 3) / 4 * 4, C.grid.cutoff_voxels, (T)C.grid.h2_over_b2,
-                     dens + C.dens_off, counts + C.counts_off, threadIdx.x & 31);
+                     (T)C.grid.gaussian_factor, dens + C.dens_off, counts + C.counts_off, threadIdx.x & 31);
 }
 
 // Workspace layout: [per-grid completion counters, n_cfgs x u32, padded to
@@ -174,7 +175,7 @@ static void launch_batched_step(const BatchLaunch &L, int bi, int bo, double *pa
     constexpr int BLOCK = 256;
     BatchStepArgs<T> b{L.cfgs, L.blk_cfg, L.blk_item0, L.blk_item1, L.cfg_blk0, L.cfg_nblk,
                        (const T *)L.pos[bi], (const T *)L.neg[bi], (T *)L.pos[bo], (T *)L.neg[bo],
-                       (const T *)L.dens[bi], (T *)L.dens[bo], L.tally, partials, counters, step};
+                       (const pair_t<T> *)L.dens[bi], (pair_t<T> *)L.dens[bo], L.tally, partials, counters, step};
     batched_step_kernel<T, BLOCK, I><<<(unsigned)L.n_blocks, BLOCK, 0, st>>>(b);
 }
 
@@ -192,11 +193,11 @@ int batched_loop(const BatchLaunch &L, cudaStream_t st) {
             if (L.dtype == PIC_F64)
                 batched_deposit_kernel<double, WARPS><<<blocks, WARPS * 32, 0, st>>>(
                     L.cfgs, L.task_cfg + t0, L.task_first + t0, L.task_prefix + t0, (int)(t1 - t0), tracks, L.xs,
-                    L.ys, (double *)L.dens[bi], L.counts);
+                    L.ys, (double2 *)L.dens[bi], L.counts);
             else
                 batched_deposit_kernel<float, WARPS><<<blocks, WARPS * 32, 0, st>>>(
                     L.cfgs, L.task_cfg + t0, L.task_first + t0, L.task_prefix + t0, (int)(t1 - t0), tracks, L.xs,
-                    L.ys, (float *)L.dens[bi], L.counts);
+                    L.ys, (float2 *)L.dens[bi], L.counts);
             int rc = check_launch("batched_deposit_kernel");
             if (rc) return rc;
         }

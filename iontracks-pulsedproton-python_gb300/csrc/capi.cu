@@ -112,7 +112,7 @@ int resolve_shape(pic_grid *g) {
                                                 " consumer warps exceed the register budget of " +
                                                 std::to_string(ipt) + " items per thread");
     }
-    const int stage_bytes = (2 * (g->tile_rows + 2) * kp + ((g->tile_rows + 8) & ~3)) * 4;
+    const int stage_bytes = (2 * (g->tile_rows + 2) * kp + 2 * ((g->tile_rows + 8) & ~3)) * 4;
     // static shared memory of the kernel (reduction scratch, flags) is < 2 KB
     const int budget = kStreamMaxSmem - 2048;
     if (g->stages <= 0) {
@@ -400,7 +400,7 @@ int pic_adjoint_forward(const pic_grid *g, void *pos0, void *neg0, void *pos1, v
     if (n_dep > 0 && !aligned(dens_keep, 16)) return set_error(PIC_E_INVALID, "dens_keep must be 16-byte aligned");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     const int64_t es = g->dtype == PIC_F64 ? 8 : 4;
-    const int64_t dslot = g->no_xy * dens_pitch(g->no_xy);
+    const int64_t dslot = 2 * g->no_xy * dens_pitch(g->no_xy);  // elements of one step's pairs
     if (n_dep > 0) {
         cudaError_t e = cudaMemsetAsync(dens_keep, 0, (size_t)(n_dep * dslot * es), st);
         if (e != cudaSuccess) return set_cuda_error("cudaMemsetAsync(dens_keep)", e);
@@ -457,7 +457,7 @@ int pic_adjoint_backward(const pic_grid *g, const void *ckpt_pos, const void *ck
     if (n_dep > 0 && !dens_keep) return set_error(PIC_E_INVALID, "dens_keep is null");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     const int64_t es = g->dtype == PIC_F64 ? 8 : 4;
-    const int64_t dslot = g->no_xy * dens_pitch(g->no_xy);
+    const int64_t dslot = 2 * g->no_xy * dens_pitch(g->no_xy);  // elements of one step's pairs
     const char *D = static_cast<const char *>(dens_keep);
     char *SP = static_cast<char *>(states_pos), *SN = static_cast<char *>(states_neg);
     // slot of every step's kept density (-1: none)

@@ -2,19 +2,20 @@
 //
 // A track is a line through the whole gap at constant LET, so its density is
 // the same in every gap layer: only the (i, j) cross-section is accumulated
-// here, and the fused step adds gaussian_factor * dens[i][j] to each gap layer
-// as it reads the fields. The cross-section is separable,
+// here (already multiplied by gaussian_factor), and the fused step adds it to
+// each gap layer as it reads the fields. The cross-section is separable,
 //   exp(-((i-x)^2 + (j-y)^2) h^2/b^2) = g_i * g_j,
 // so a track costs one exponential per stencil row and column and one multiply
 // per cell (the identities of solver_numba.py:10-26). The stencil box is
 // [ceil(x - cut), floor(x + cut)] clipped to [0, no_xy), as in
 // solver_numba.py:86-89.
 //
-// The density is laid out [no_xy][dens_pitch(no_xy)] (rows padded to 16
-// bytes). One to eight warps per track (more when the step has few tracks),
-// splitting the box's rows. Lanes own stencil columns j; row factors are
-// computed 32 rows at a time, one row per lane, and broadcast by shuffle. Each cell is
-// added with a float atomic: tracks overlap, and the L2 resolves the
+// The deposition is laid out [no_xy][dens_pitch(no_xy)] pairs (G * density,
+// G * the density of the four lateral neighbours; rows padded to 4 pairs).
+// One to eight warps per track (more when the step has few tracks), splitting
+// the box's rows. Lanes own stencil columns j; row factors are computed 32
+// rows at a time, one row per lane, and broadcast by shuffle. Each cell's pair
+// is added with one vector atomic: tracks overlap, and the L2 resolves the
 // collisions. The offset (i - x) is formed in float64 from the float64 track
 // centre before it is rounded, so the Gaussian is not shifted by the float32
 // spacing of x (up to 6e-5 voxel at x ~ 1000).
@@ -32,12 +33,13 @@ namespace pic {
 template <typename T, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) deposit_kernel(const double *__restrict__ xs,
                                                               const double *__restrict__ ys, int64_t m,
-                                                              T *__restrict__ dens, uint32_t *__restrict__ counts,
-                                                              int64_t n, int64_t dp, double cut, T h2b2, int parts) {
+                                                              pair_t<T> *__restrict__ dens,
+                                                              uint32_t *__restrict__ counts, int64_t n, int64_t dp,
+                                                              double cut, T h2b2, T gfac, int parts) {
     const int warp = threadIdx.x >> 5;
     const int64_t t = (int64_t)blockIdx.x * (WARPS / parts) + warp / parts;
     if (t >= m) return;
-    deposit_track<T>(xs[t], ys[t], n, dp, cut, h2b2, dens, counts, threadIdx.x & 31, warp % parts, parts);
+    deposit_track<T>(xs[t], ys[t], n, dp, cut, h2b2, gfac, dens, counts, threadIdx.x & 31, warp % parts, parts);
 }
 
 // Warps per track: a step's tracks alone rarely fill the GPU (a few to a few
@@ -58,12 +60,12 @@ int launch_deposit(const pic_grid *g, const double *xs, const double *ys, int64_
     const int64_t blocks = (m + per_block - 1) / per_block;
     if (g->dtype == PIC_F64) {
         deposit_kernel<double, WARPS><<<(unsigned)blocks, WARPS * 32, 0, st>>>(
-            xs, ys, m, (double *)dens, counts, g->no_xy, dens_pitch(g->no_xy), g->cutoff_voxels, g->h2_over_b2,
-            parts);
+            xs, ys, m, (double2 *)dens, counts, g->no_xy, dens_pitch(g->no_xy), g->cutoff_voxels, g->h2_over_b2,
+            g->gaussian_factor, parts);
     } else {
         deposit_kernel<float, WARPS><<<(unsigned)blocks, WARPS * 32, 0, st>>>(
-            xs, ys, m, (float *)dens, counts, g->no_xy, dens_pitch(g->no_xy), g->cutoff_voxels,
-            (float)g->h2_over_b2, parts);
+            xs, ys, m, (float2 *)dens, counts, g->no_xy, dens_pitch(g->no_xy), g->cutoff_voxels,
+            (float)g->h2_over_b2, (float)g->gaussian_factor, parts);
     }
     return check_launch("deposit_kernel");
 }

@@ -13,13 +13,13 @@
 // outputs (next fields, track histogram, tallies).
 //
 // Limits and behaviour:
-//   * the array holds the 2D density (rows padded to 4 elements) of up to
-//     kNoAllocDensBytes (8 MiB): no_xy <= 1448 for float32 fields, <= 1024
-//     for float64; larger grids are refused with PIC_E_CAPACITY;
-//   * every GPU that loads the library holds the array (8 MiB + the tally
+//   * the array holds the 2D deposition pairs (rows padded to 4 pairs) of up
+//     to kNoAllocDensBytes (16 MiB): no_xy <= 1448 for float32 fields,
+//     <= 1024 for float64; larger grids are refused with PIC_E_CAPACITY;
+//   * every GPU that loads the library holds the array (16 MiB + the tally
 //     workspace) until the process exits;
 //   * every call shares the array and it keeps the last call's contents: the
-//     density is cleared at the start of each call, the tally counter is
+//     pairs are cleared at the start of each call, the tally counter is
 //     left at zero by each completed step;
 //   * calls that overlap on the GPU (different streams, or different host
 //     threads) race on the array and give wrong results: serialise them;
@@ -36,10 +36,11 @@
 
 namespace pic {
 
-constexpr int64_t kNoAllocDensBytes = 8LL << 20;
+constexpr int64_t kNoAllocDensBytes = 16LL << 20;
 constexpr int64_t kNoAllocScratchBytes = kNoAllocDensBytes + kWorkspaceBytes;
 
-// Device scratch of pic_step_noalloc: [2D density (8 MiB) | tally workspace].
+// Device scratch of pic_step_noalloc: [2D deposition pairs (16 MiB) | tally
+// workspace].
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 // Device address of the array, looked up once per device with that device
@@ -66,7 +67,7 @@ int step_noalloc(const pic_grid *g, const void *pos_in, const void *neg_in, void
                  const double *xs, const double *ys, int64_t n_tracks, uint32_t *counts, double *tally,
                  cudaStream_t st) {
     const int64_t es = g->dtype == PIC_F64 ? 8 : 4;
-    const int64_t dens_bytes = g->no_xy * dens_pitch(g->no_xy) * es;
+    const int64_t dens_bytes = 2 * g->no_xy * dens_pitch(g->no_xy) * es;  // deposition pairs
     if (dens_bytes > kNoAllocDensBytes)
         return set_error(PIC_E_CAPACITY,
                          "pic_step_noalloc: the 2D density of a " + std::to_string(g->no_xy) + " x " +

@@ -37,6 +37,15 @@ __device__ __forceinline__ void store4(double *p, const V4<double> &v) {
     reinterpret_cast<double2 *>(p)[1] = make_double2(v.v[2], v.v[3]);
 }
 
+// One cell of the 2D deposition of a step: (G * density, G * the sum of the
+// density of its four lateral neighbours), G the track peak density. The step
+// kernels add the first to the cell's gap layers and the second to the
+// lateral sum of its stencil, one load per column.
+template <typename T> struct PairOf;
+template <> struct PairOf<float> { using type = float2; };
+template <> struct PairOf<double> { using type = double2; };
+template <typename T> using pair_t = typename PairOf<T>::type;
+
 // Running sum of one tally. FP32 partials are Kahan-compensated: a thread
 // adds thousands of voxel values, and plain float accumulation would lose
 // ~1e-5 of the total; the compensation keeps it at float64-like accuracy

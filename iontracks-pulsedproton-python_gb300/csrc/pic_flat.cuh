@@ -15,8 +15,8 @@ template <typename T>
 struct StepArgs {
     const T *pos_in, *neg_in;
     T *pos_out, *neg_out;
-    const T *dens;   // null: no deposition this step
-    T *dens_zero;    // null: nothing to clear
+    const pair_t<T> *dens;  // the step's deposition pairs (null: none)
+    pair_t<T> *dens_zero;   // the next step's pairs, cleared here (null: none)
     double *tally;
     double *partials;
     unsigned int *counter;
@@ -25,12 +25,12 @@ struct StepArgs {
     int reflecting;
     T p_lat, p_zm, p_zp, p_cen, n_lat, n_zm, n_zp, n_cen, alpha_dt, gfac;
     ScoreTest score;
-    double injected_scale;
+    double injected_scale;  // no_z: the pairs carry G already
 };
 
 template <typename T>
 __device__ __forceinline__ T dep_at(const StepArgs<T> &a, int64_t dcol) {
-    return a.dens ? a.gfac * a.dens[dcol] : T(0);
+    return a.dens ? a.dens[dcol].x : T(0);
 }
 
 // Index type of a grid: 32-bit unsigned offsets when every element offset of
@@ -63,7 +63,7 @@ __device__ __forceinline__ void flat_item(const StepArgs<T> &a, I item, Tally<T>
     const int c = (int)(item - col * c4);
     const I i = col / n, j = col - i * n;
     const int k0 = 4 * c;
-    if (c == 0 && a.dens_zero) a.dens_zero[i * dp + j] = T(0);
+    if (c == 0 && a.dens_zero) a.dens_zero[i * dp + j] = pair_t<T>{T(0), T(0)};
 
     // gap mask of the four outputs and of the two z-neighbours
     bool g[4];
@@ -104,18 +104,18 @@ __device__ __forceinline__ void flat_item(const StepArgs<T> &a, I item, Tally<T>
     T nkp = k0 + 4 < kp ? a.neg_in[base + 4] : T(0);
 
     const I dcol = ci * dp + cj;
+    // this column's deposition and its neighbours' (gap layers only): one
+    // pair per column
+    T dc = T(0), dl = T(0);
     if (a.dens) {
-        const T dc = a.gfac * a.dens[dcol];
-        const T dim = a.gfac * a.dens[dcol - dp], dip = a.gfac * a.dens[dcol + dp];
-        const T djm = a.gfac * a.dens[dcol - 1], djp = a.gfac * a.dens[dcol + 1];
+        const pair_t<T> d = a.dens[dcol];
+        dc = d.x;
+        dl = d.y;
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
             if (g[e]) {
-                P.v[e] += dc; N.v[e] += dc;
-                Pim.v[e] += dim; Nim.v[e] += dim;
-                Pip.v[e] += dip; Nip.v[e] += dip;
-                Pjm.v[e] += djm; Njm.v[e] += djm;
-                Pjp.v[e] += djp; Njp.v[e] += djp;
+                P.v[e] += dc;
+                N.v[e] += dc;
             }
         }
         if (g_km) { pkm += dc; nkm += dc; }
@@ -133,10 +133,11 @@ __device__ __forceinline__ void flat_item(const StepArgs<T> &a, I item, Tally<T>
         const T p_kp1 = e < 3 ? P.v[e + 1] : pkp;
         const T n_km1 = e > 0 ? N.v[e - 1] : nkm;
         const T n_kp1 = e < 3 ? N.v[e + 1] : nkp;
+        const T dle = g[e] ? dl : T(0);
         const T p_new = a.p_zm * p_km1 + a.p_zp * p_kp1 +
-                        a.p_lat * ((Pjm.v[e] + Pjp.v[e]) + (Pim.v[e] + Pip.v[e])) + a.p_cen * p;
+                        a.p_lat * (((Pjm.v[e] + Pjp.v[e]) + (Pim.v[e] + Pip.v[e])) + dle) + a.p_cen * p;
         const T n_new = a.n_zm * n_kp1 + a.n_zp * n_km1 +
-                        a.n_lat * ((Njm.v[e] + Njp.v[e]) + (Nim.v[e] + Nip.v[e])) + a.n_cen * nn;
+                        a.n_lat * (((Njm.v[e] + Njp.v[e]) + (Nim.v[e] + Nip.v[e])) + dle) + a.n_cen * nn;
         const T rec = a.alpha_dt * p * nn;
         const bool valid = (k >= 1) && (k <= a.nzb - 2);
         const T po = valid ? p_new - rec : T(0);
@@ -155,7 +156,7 @@ __device__ __forceinline__ void flat_item(const StepArgs<T> &a, I item, Tally<T>
         t_rec.add(rec_sum);
         t_p.add(p_sum);
         t_n.add(n_sum);
-        if (c == 0 && a.dens) t_inj.add(a.dens[dcol]);
+        if (c == 0 && a.dens) t_inj.add(dc);
     }
 }
 

@@ -10,16 +10,18 @@
 //   outer ring, reflecting wall: the new value of the nearest interior column
 //     (the reference's i-planes-then-j-planes mirror, state.py:151-154, which
 //     maps corners to the diagonal interior column).
-// The step's deposition (gaussian_factor * dens[i][j], gap layers only) is
-// added to every value as it is read, the fused form of the reference's
-// separate broadcast pass (solver_numba_parallel.py:222-277). The z end planes
+// The step's deposition is added to every value as it is read (gap layers
+// only), the fused form of the reference's separate broadcast pass
+// (solver_numba_parallel.py:222-277): each column reads one pair, its own
+// G * density (added to its values) and the sum over its four lateral
+// neighbours (added to the stencil's lateral sum). The z end planes
 // k = 0 and k >= nzb-1 (and the row padding) are written as zero.
 //
 // Tallies over the scored set (interior, inside scoring_radius_sq, gap
 // layers) follow _lax_wendroff_step_numba (solver_numba.py:204-211):
 // recombined uses the pre-step densities, n+/n- the updated ones. The
-// injected charge of the step is sum(dens) over scored columns times
-// gaussian_factor * no_z (solver_numba_parallel.py:271-276).
+// injected charge of the step is sum(G * density) over scored columns times
+// no_z (solver_numba_parallel.py:271-276).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -54,8 +56,8 @@ static int launch_step_t(const pic_grid *g, const void *pos_in, const void *neg_
     a.neg_in = (const T *)neg_in;
     a.pos_out = (T *)pos_out;
     a.neg_out = (T *)neg_out;
-    a.dens = (const T *)dens;
-    a.dens_zero = (T *)dens_zero;
+    a.dens = (const pair_t<T> *)dens;
+    a.dens_zero = (pair_t<T> *)dens_zero;
     a.tally = tally;
     Workspace w = workspace_layout(ws);
     a.partials = w.partials;
@@ -75,7 +77,7 @@ static int launch_step_t(const pic_grid *g, const void *pos_in, const void *neg_
     a.gfac = (T)g->gaussian_factor;
     int rc = score_test(g, &a.score);
     if (rc) return rc;
-    a.injected_scale = g->gaussian_factor * (double)g->no_z;
+    a.injected_scale = (double)g->no_z;
     int64_t blocks = (a.items + BLOCK - 1) / BLOCK;
     const int64_t cap = step_grid_cap(g->dtype == PIC_F64 ? 1 : 0);
     if (blocks > cap) blocks = cap;

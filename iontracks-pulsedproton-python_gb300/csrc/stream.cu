@@ -33,13 +33,13 @@ namespace pic {
 struct StreamArgs {
     const float *pos_in, *neg_in;
     float *pos_out, *neg_out;
-    const float *dens;  // null: no deposition this step
-    float *dens_zero;   // null: nothing to clear
+    const float2 *dens;  // deposition pairs (G * density, G * neighbours'); null: none
+    float2 *dens_zero;   // the next step's pairs, cleared here; null: nothing to clear
     double *tally, *partials;
     unsigned int *counter;
     int *status;
     int n, kp, c4, nzb, nze, gap_end, reflecting;
-    int dp;  // density row pitch (multiple of 4 elements)
+    int dp;  // deposition row pitch (multiple of 4 pairs)
     int tj, li, jt, n_items, stages, consumer_warps;
     float p_lat, p_zm, p_zp, p_cen, n_lat, n_zm, n_zp, n_cen, alpha_dt, gfac;
     int two_mid;    // 2 * mid_xy
@@ -113,8 +113,8 @@ __global__ void __launch_bounds__(stream_max_threads(IPT), 1) stream_step_kernel
     float *stage0 = reinterpret_cast<float *>(smem_raw + bar_bytes);
     const int rows_max = a.tj + 2;
     const int spec = rows_max * a.kp;       // floats per species in a stage
-    const int dens_off = 2 * spec;          // the plane's density row segment
-    const int stage_floats = 2 * spec + ((a.tj + 8) & ~3);
+    const int dens_off = 2 * spec;          // the plane's deposition pairs (float offset)
+    const int stage_floats = 2 * spec + 2 * ((a.tj + 8) & ~3);
     const bool has_dens = a.dens != nullptr;
     const int S = a.stages;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -137,8 +137,9 @@ __global__ void __launch_bounds__(stream_max_threads(IPT), 1) stream_step_kernel
     if (warp == cw) {
         // ---------------- producer warp: lane 0 issues every copy ----------------
         // Per plane: the tile's rows (plus j-halo) of both species, and the
-        // plane's density over the same rows, fetched from its 16-byte-aligned
-        // cover [a0, a0 + 4 * ceil((off + rows) / 4)) of the padded row.
+        // plane's deposition pairs over the same rows, fetched from their
+        // 32-byte-aligned cover [a0, a0 + 4 * ceil((off + rows) / 4)) of the
+        // padded row.
         if (lane == 0) {
             long long g = 0;
             bool ok = true;
@@ -148,7 +149,7 @@ __global__ void __launch_bounds__(stream_max_threads(IPT), 1) stream_step_kernel
                 const int rows = cj_hi - cj_lo + 2;
                 const uint32_t bytes = (uint32_t)(rows * a.kp * 4);
                 const int doff = (cj_lo - 1) & 3;
-                const uint32_t dbytes = has_dens ? (uint32_t)(((doff + rows + 3) & ~3) * 4) : 0u;
+                const uint32_t dbytes = has_dens ? (uint32_t)(((doff + rows + 3) & ~3) * 8) : 0u;
                 for (int pl = ci_lo - 1; pl <= ci_hi; ++pl, ++g) {
                     const int slot = (int)(g % S);
                     if (g >= S && !mbar_wait(&empty[slot], (uint32_t)(((g / S) - 1) & 1), a.status, 1)) {
@@ -209,7 +210,7 @@ __global__ void __launch_bounds__(stream_max_threads(IPT), 1) stream_step_kernel
             const int nplanes = ci_hi - ci_lo + 2;
             const int rows_out = cj_hi - cj_lo;
             const int n_core = rows_out * ncore, n_all = rows_out * c4;
-            const int dbase = dens_off + ((cj_lo - 1) & 3);  // density of staged row q: dbase + q
+            const int dq = (cj_lo - 1) & 3;  // pair of staged row q: dq + q
             // per-slot constants: kind (0 dead, 1 core, 2 edge), row+1, vector
             int kind[IPT], rs_[IPT], c_[IPT];
             uint32_t dy2[IPT];
@@ -262,11 +263,11 @@ __global__ void __launch_bounds__(stream_max_threads(IPT), 1) stream_step_kernel
                     const int o = rs * kp + k0;
                     // convergent part: centre vectors, densities, edge shuffles
                     float4 P = lds4(Sc + o), N = lds4(Sc + spec + o);
-                    const float dens_c = has_dens ? Sc[dbase + rs] : 0.f;
-                    const float dcen = a.gfac * dens_c;
-                    const float dlat = has_dens ? a.gfac * ((Sc[dbase + rs - 1] + Sc[dbase + rs + 1]) +
-                                                            (Sm[dbase + rs] + Sp[dbase + rs]))
-                                                : 0.f;
+                    const float2 dpair = has_dens ? reinterpret_cast<const float2 *>(Sc + dens_off)[dq + rs]
+                                                  : make_float2(0.f, 0.f);
+                    const float dens_c = dpair.x;  // G * density of this column
+                    const float dcen = dens_c;
+                    const float dlat = dpair.y;    // G * density of its four neighbours
                     if (kd == 1) {
                         P.x += dcen; P.y += dcen; P.z += dcen; P.w += dcen;
                         N.x += dcen; N.y += dcen; N.z += dcen; N.w += dcen;
@@ -380,10 +381,9 @@ __global__ void __launch_bounds__(stream_max_threads(IPT), 1) stream_step_kernel
                         }
                         PO = make_float4(po[0], po[1], po[2], po[3]);
                         NO = make_float4(no[0], no[1], no[2], no[3]);
-                        const int64_t ccol = (int64_t)ci * n + cj;
                         if (c == 0) {
                             if (scored && has_dens) t_inj.add(dens_c);
-                            if (a.dens_zero) a.dens_zero[(int64_t)ci * a.dp + cj] = 0.f;
+                            if (a.dens_zero) a.dens_zero[(int64_t)ci * a.dp + cj] = make_float2(0.f, 0.f);
                         }
                     }
                     const int out = cj * kp + k0;
@@ -420,7 +420,7 @@ __global__ void __launch_bounds__(stream_max_threads(IPT), 1) stream_step_kernel
                                 st4(a.neg_out + rcol * kp + k0, NO);
                             } else {
                                 float4 RP = lds4(Sr + row * kp + k0), RN = lds4(Sr + spec + row * kp + k0);
-                                const float d = has_dens ? a.gfac * Sr[dbase + row] : 0.f;
+                                const float d = has_dens ? reinterpret_cast<const float2 *>(Sr + dens_off)[dq + row].x : 0.f;
 #pragma unroll
                                 for (int e = 0; e < 4; ++e) {
                                     const int kk = k0 + e;
@@ -431,7 +431,7 @@ __global__ void __launch_bounds__(stream_max_threads(IPT), 1) stream_step_kernel
                                 st4(a.pos_out + rcol * kp + k0, RP);
                                 st4(a.neg_out + rcol * kp + k0, RN);
                             }
-                            if (c == 0 && a.dens_zero) a.dens_zero[(int64_t)ri * a.dp + rj] = 0.f;
+                            if (c == 0 && a.dens_zero) a.dens_zero[(int64_t)ri * a.dp + rj] = make_float2(0.f, 0.f);
                         }
                     }
                 }
@@ -474,7 +474,7 @@ static int launch_ipt(const StreamArgs &a, unsigned blocks, int threads, int sme
 }
 
 int stream_smem_bytes(int tj, int kp, int stages) {
-    return (2 * stages * 8 + 127) / 128 * 128 + stages * (2 * (tj + 2) * kp + ((tj + 8) & ~3)) * 4;
+    return (2 * stages * 8 + 127) / 128 * 128 + stages * (2 * (tj + 2) * kp + 2 * ((tj + 8) & ~3)) * 4;
 }
 
 int launch_stream_step(const pic_grid *g, const StreamShape &sh, const void *pos_in, const void *neg_in,
@@ -485,8 +485,8 @@ int launch_stream_step(const pic_grid *g, const StreamShape &sh, const void *pos
     a.neg_in = (const float *)neg_in;
     a.pos_out = (float *)pos_out;
     a.neg_out = (float *)neg_out;
-    a.dens = (const float *)dens;
-    a.dens_zero = (float *)dens_zero;
+    a.dens = (const float2 *)dens;
+    a.dens_zero = (float2 *)dens_zero;
     a.tally = tally;
     Workspace w = workspace_layout(ws);
     a.partials = w.partials;
@@ -518,7 +518,7 @@ int launch_stream_step(const pic_grid *g, const StreamShape &sh, const void *pos
     a.two_mid = (int)sc.two_mid;
     // (2i - two_mid)^2 + (2j - two_mid)^2 < 2^31 for no_xy <= 16383
     a.thr4 = sc.thr4 < 0 ? 0u : (sc.thr4 > 0x7fffffffLL ? 0xffffffffu : (uint32_t)sc.thr4);
-    a.injected_scale = g->gaussian_factor * (double)g->no_z;
+    a.injected_scale = (double)g->no_z;  // the pairs carry G already
     const int smem = stream_smem_bytes(a.tj, a.kp, a.stages);
     int64_t blocks = (int64_t)sh.sm_count * sh.ctas_per_sm;
     if (blocks > a.n_items) blocks = a.n_items;

@@ -78,7 +78,7 @@ def device_bytes(config, dtype: str = "float32", max_tracks: int = 0) -> int:
     kp = (int(config.no_z_with_buffer) + 7) // 8 * 8
     es = 4 if dtype == "float32" else 8
     dp = (n + 3) // 4 * 4
-    return 4 * n * n * kp * es + 2 * n * dp * es + n * n * 4 + int(config.total_time_steps) * 32 + 16 * max_tracks
+    return 4 * n * n * kp * es + 4 * n * dp * es + n * n * 4 + int(config.total_time_steps) * 32 + 16 * max_tracks
 
 
 class ChamberEngine:
@@ -110,9 +110,10 @@ class ChamberEngine:
         kw = dict(device=self.device)
         self.pos = [torch.zeros(shape, dtype=tdt, **kw), torch.zeros(shape, dtype=tdt, **kw)]
         self.neg = [torch.zeros(shape, dtype=tdt, **kw), torch.zeros(shape, dtype=tdt, **kw)]
-        # 2D density, rows padded to 4 elements (pic_dens_pitch)
+        # deposition pairs (G * density, G * neighbours' sum), rows padded to
+        # 4 pairs (pic_dens_pitch)
         self.dens_pitch = (g.no_xy + 3) // 4 * 4
-        self.dens = [torch.zeros((g.no_xy, self.dens_pitch), dtype=tdt, **kw) for _ in range(2)]
+        self.dens = [torch.zeros((g.no_xy, 2 * self.dens_pitch), dtype=tdt, **kw) for _ in range(2)]
         self.counts = torch.zeros((g.no_xy, g.no_xy), dtype=torch.int32, **kw)
         steps = int(config.total_time_steps) if tally_steps is None else int(tally_steps)
         self.tally = torch.zeros((max(steps, 1), 4), dtype=torch.float64, **kw)

@@ -180,8 +180,17 @@ def test_kernel_level_deposit_and_step(name):
         inner = (slice(1, -1), slice(1, -1), slice(None))
         np.testing.assert_allclose(pos[inner], ref_pos[inner], rtol=0, atol=peak * tol)
         np.testing.assert_allclose(neg[inner], fx["negative_next"][inner], rtol=0, atol=peak * tol)
-        dens = eng.dens[0][:, :cfg.no_xy].cpu().numpy().astype(np.float64)
-        np.testing.assert_allclose(dens, fx["total_density"], rtol=tol, atol=tol * fx["total_density"].max())
+        # deposition pairs: (G * density, G * the four lateral neighbours' density)
+        n, G = int(cfg.no_xy), float(cfg.Gaussian_factor)
+        pairs = eng.dens[0].view(n, -1, 2)[:, :n].cpu().numpy().astype(np.float64)
+        ref = fx["total_density"]
+        np.testing.assert_allclose(pairs[..., 0] / G, ref, rtol=tol, atol=tol * ref.max())
+        lat = np.zeros_like(ref)
+        lat[1:] += ref[:-1]
+        lat[:-1] += ref[1:]
+        lat[:, 1:] += ref[:, :-1]
+        lat[:, :-1] += ref[:, 1:]
+        np.testing.assert_allclose(pairs[..., 1] / G, lat, rtol=tol, atol=tol * lat.max())
         eng.close()
 
 

@@ -57,7 +57,7 @@ def test_two_calls_match_the_allocating_entry_points(dtype, wall):
 
     # allocating path: caller-owned density and workspace
     fa = [torch.zeros(shape, dtype=tdt, device=dev) for _ in range(6)]  # pos/neg x 3 time levels
-    dens = torch.zeros((g.no_xy, lib.pic_dens_pitch(g.no_xy)), dtype=tdt, device=dev)
+    dens = torch.zeros((g.no_xy, 2 * lib.pic_dens_pitch(g.no_xy)), dtype=tdt, device=dev)  # pairs
     wsb = ctypes.c_int64()
     N.check(lib.pic_step_workspace_bytes(ctypes.byref(g), ctypes.byref(wsb)), "pic_step_workspace_bytes")
     ws = torch.zeros(int(wsb.value), dtype=torch.uint8, device=dev)
@@ -100,7 +100,7 @@ def test_grid_beyond_the_static_scratch_is_refused():
     lib = N.load()
     cfg = make_config("full_electrode_5um_10p", sampled_radius_cm=0.4)  # no_xy = 1608 > 1448
     g = eng.make_grid(cfg)
-    assert g.no_xy * lib.pic_dens_pitch(g.no_xy) * 4 > 8 << 20
+    assert 2 * g.no_xy * lib.pic_dens_pitch(g.no_xy) * 4 > 16 << 20
     small = [torch.zeros(8, dtype=torch.float32, device="cuda") for _ in range(4)]
     tally = torch.zeros(4, dtype=torch.float64, device="cuda")
     counts = torch.zeros(1, dtype=torch.int32, device="cuda")
