@@ -207,6 +207,18 @@ int pic_sample_disc_pcg64(uint64_t *state, double scale, double mid, double radi
                           int64_t max_pairs, double *xs, double *ys, int64_t *n_accepted, int64_t *n_draws);
 
 /*
+ * pic_arrival_counts_pcg64 -- tracks arriving in each time step of one pulse
+ * (host, no GPU), replacing pulse_arrival_counts (pulsed_ion_chamber/pulses.py:
+ * 39-61) for a NumPy PCG64 generator: n uniforms drawn as random(n) draws
+ * them, arrival = cumsum / cumsum[-1] * duration, then counts[b] = the
+ * arrivals in [edges[b], edges[b+1]) (the last bin closed), as np.histogram
+ * over the n_edges edges; bit-identical. Advances state[0..1] past the n
+ * draws.
+ */
+int pic_arrival_counts_pcg64(uint64_t *state, int64_t n, double duration, const double *edges, int64_t n_edges,
+                             int64_t *counts);
+
+/*
  * Adjoint of the fused step (no counterpart in the reference, which has no
  * derivatives): reverse-mode derivatives of R, the run's total recombined
  * charge, for k_s = I / (I - R).

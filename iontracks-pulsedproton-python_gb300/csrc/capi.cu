@@ -335,6 +335,16 @@ int pic_sample_disc(const double *u, int64_t n_pairs, double scale, double mid, 
     return sample_disc(u, n_pairs, scale, mid, radius_sq, n_wanted, xs, ys, n_accepted, n_pairs_used);
 }
 
+int pic_arrival_counts_pcg64(uint64_t *state, int64_t n, double duration, const double *edges, int64_t n_edges,
+                             int64_t *counts) {
+    if (!state || !edges || !counts) return set_error(PIC_E_INVALID, "null pointer argument");
+    if (n < 1 || n_edges < 2) return set_error(PIC_E_INVALID, "n must be >= 1 and n_edges >= 2");
+    if ((state[3] & 1u) == 0u) return set_error(PIC_E_INVALID, "a PCG64 increment is odd");
+    for (int64_t b = 0; b + 1 < n_edges; ++b)
+        if (!(edges[b] <= edges[b + 1])) return set_error(PIC_E_INVALID, "edges must be non-decreasing");
+    return arrival_counts_pcg64(state, n, duration, edges, n_edges, counts);
+}
+
 int pic_sample_disc_pcg64(uint64_t *state, double scale, double mid, double radius_sq, int64_t n_wanted,
                           int64_t max_pairs, double *xs, double *ys, int64_t *n_accepted, int64_t *n_draws) {
     if (!state || !n_accepted || !n_draws) return set_error(PIC_E_INVALID, "null pointer argument");

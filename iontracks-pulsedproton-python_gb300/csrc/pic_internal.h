@@ -104,6 +104,8 @@ int adjoint_accumulate_end(const pic_grid *g, void *ws, double *grad, cudaStream
 
 int sample_disc(const double *u, int64_t n_pairs, double scale, double mid, double radius_sq, int64_t n_wanted,
                 double *xs, double *ys, int64_t *n_accepted, int64_t *n_pairs_used);
+int arrival_counts_pcg64(uint64_t *st, int64_t n, double duration, const double *edges, int64_t n_edges,
+                         int64_t *counts);
 int sample_disc_pcg64(uint64_t *st, double scale, double mid, double radius_sq, int64_t n_wanted, int64_t max_pairs,
                       double *xs, double *ys, int64_t *n_accepted, int64_t *n_draws);
 

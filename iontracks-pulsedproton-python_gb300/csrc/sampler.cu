@@ -90,4 +90,37 @@ int sample_disc_pcg64(uint64_t *st, double scale, double mid, double radius_sq, 
     return PIC_OK;
 }
 
+// Arrival counts of one pulse (pulsed_ion_chamber/pulses.py:39-61) from a
+// PCG64 state: n uniforms u_k drawn as NumPy's random(n) draws them, their
+// running sum S_k (left to right, as np.cumsum), arrival a_k = (S_k / S_{n-1})
+// * duration (as the in-place divide and multiply), then per bin b the
+// count of a_k in [edges[b], edges[b+1]) -- the last bin closed on the right --
+// which is what np.histogram counts over explicit edges. The stream is drawn
+// twice from the same state, first for S_{n-1}, then to bin each a_k as it is
+// formed (a_k is non-decreasing, so one bin pointer moves forward): no
+// n-element buffer.
+int arrival_counts_pcg64(uint64_t *st, int64_t n, double duration, const double *edges, int64_t n_edges,
+                         int64_t *counts) {
+    const Pcg64 start{((u128)st[0] << 64) | st[1], ((u128)st[2] << 64) | st[3]};
+    Pcg64 r = start;
+    double last = 0.0;
+    for (int64_t k = 0; k < n; ++k) last += r.next_double();
+    const int64_t nb = n_edges - 1;
+    for (int64_t q = 0; q < nb; ++q) counts[q] = 0;
+    r = start;
+    double s = 0.0;
+    int64_t bin = 0;
+    for (int64_t k = 0; k < n; ++k) {
+        s += r.next_double();
+        const double q = s / last;
+        const double t = q * duration;
+        if (t < edges[0]) continue;
+        while (bin < nb - 1 && t >= edges[bin + 1]) ++bin;
+        if (bin < nb - 1 || t <= edges[nb]) ++counts[bin];
+    }
+    st[0] = (uint64_t)(r.state >> 64);
+    st[1] = (uint64_t)r.state;
+    return PIC_OK;
+}
+
 }  // namespace pic

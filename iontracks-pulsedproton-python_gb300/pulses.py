@@ -34,6 +34,8 @@ def pulse_arrival_counts(config, rng: np.random.Generator) -> np.ndarray:
     """Tracks arriving in each time step of one pulse (int64, length
     ``pulse_time_steps``)."""
     n = int(config.number_of_tracks_per_pulse)
+    if n >= 1 and type(rng.bit_generator) is np.random.PCG64:
+        return _arrival_counts_pcg64(config, rng, n)
     arrival = np.cumsum(rng.random(n))
     arrival /= arrival[-1]
     arrival *= config.pulse_duration_s
@@ -46,6 +48,33 @@ def pulse_arrival_counts(config, rng: np.random.Generator) -> np.ndarray:
     cum = np.concatenate([np.searchsorted(arrival, bins[:-1], side="left"),
                           np.searchsorted(arrival, bins[-1:], side="right")])
     return np.diff(cum).astype(np.int64)
+
+
+def _pcg64_state(rng):
+    d = rng.bit_generator.state
+    s, inc = int(d["state"]["state"]), int(d["state"]["inc"])
+    m64 = (1 << 64) - 1
+    return d, np.array([s >> 64, s & m64, inc >> 64, inc & m64], dtype=np.uint64)
+
+
+def _store_pcg64_state(rng, d, st) -> None:
+    d["state"]["state"] = (int(st[0]) << 64) | int(st[1])
+    rng.bit_generator.state = d
+
+
+def _arrival_counts_pcg64(config, rng, n: int) -> np.ndarray:
+    """The same counts drawn and binned natively (``pic_arrival_counts_pcg64``:
+    the same doubles, the same left-to-right running sum and the same
+    divide-then-multiply, each arrival binned as it is formed); the generator
+    is left past the n draws."""
+    lib = N.load()
+    edges = np.ascontiguousarray(config.pulse_time_bins, dtype=np.float64)
+    counts = np.zeros(len(edges) - 1, dtype=np.int64)
+    d, st = _pcg64_state(rng)
+    N.check(lib.pic_arrival_counts_pcg64(st.ctypes.data, n, float(config.pulse_duration_s), edges.ctypes.data,
+                                         len(edges), counts.ctypes.data), "pic_arrival_counts_pcg64")
+    _store_pcg64_state(rng, d, st)
+    return counts
 
 
 def build_track_schedule(config, rng: np.random.Generator) -> np.ndarray:
@@ -130,11 +159,7 @@ class TrackSampler:
         generator ends exactly past the doubles consumed, so the next call
         (or any later draw) continues the stream."""
         lib = N.load()
-        bg = self.rng.bit_generator
-        d = bg.state
-        s, inc = int(d["state"]["state"]), int(d["state"]["inc"])
-        m64 = (1 << 64) - 1
-        st = np.array([s >> 64, s & m64, inc >> 64, inc & m64], dtype=np.uint64)
+        d, st = _pcg64_state(self.rng)
         xs_out = np.empty(n_tracks)
         ys_out = np.empty(n_tracks)
         acc, draws = ctypes.c_int64(), ctypes.c_int64()
@@ -148,8 +173,7 @@ class TrackSampler:
                                               xs_out[filled:].ctypes.data, ys_out[filled:].ctypes.data,
                                               ctypes.byref(acc), ctypes.byref(draws)), "pic_sample_disc_pcg64")
             filled += acc.value
-        d["state"]["state"] = (int(st[0]) << 64) | int(st[1])
-        bg.state = d
+        _store_pcg64_state(self.rng, d, st)
         return xs_out, ys_out
 
 

@@ -98,19 +98,22 @@ def test_native_disc_scan_equals_the_numpy_expression():
 
 
 def test_arrival_counts_equal_numpy_histogram():
-    """The per-step arrival histogram (binary searches on the sorted arrival
-    times) equals np.histogram over the same edges (pulses.py:39-61), for the
-    golden configurations, the sweep and extra seeds."""
+    """The per-step arrival histogram (drawn and binned natively for a PCG64
+    generator) equals np.histogram over the same edges (pulses.py:39-61), for
+    the golden configurations, the sweep and extra seeds, and leaves the
+    generator where NumPy's own draws leave it."""
     cfgs = [make_config(n) for n in NAMES] + pkg().saturation_sweep_configs()
     for cfg in cfgs:
         for seed in (cfg.seed, 7):
-            a = importlib.import_module(pkg().__name__ + ".pulses").pulse_arrival_counts(cfg, np.random.default_rng(seed))
+            mine = np.random.default_rng(seed)
+            a = importlib.import_module(pkg().__name__ + ".pulses").pulse_arrival_counts(cfg, mine)
             rng = np.random.default_rng(seed)
             arrival = np.cumsum(rng.random(int(cfg.number_of_tracks_per_pulse)))
             arrival /= arrival[-1]
             arrival *= cfg.pulse_duration_s
             ref, _ = np.histogram(arrival, cfg.pulse_time_bins)
             np.testing.assert_array_equal(a, ref)
+            assert mine.random() == rng.random()  # the generator continues at the same point
 
 
 @pytest.mark.parametrize("geom", [(60, 30, 24.0), (25, 12.5, 9.5), (95, 47.5, 43.5), (7, 3.5, 3.5)])
