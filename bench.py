@@ -179,16 +179,19 @@ def run_reference(args):
     if rank != 0:
         return 0
     desc, cfg = _config(args.workload)
-    steps = max(1, args.ref_steps)
-    v, cores, wall = cpu_sample(cfg, steps=steps, warmup=min(args.warmup, 2))
+    # K timed steps after W untimed ones, bounded (about 0.2 s per full-electrode
+    # step on 16 cores) so that the run ends within a few minutes
+    steps = max(1, min(args.steps, args.ref_max_steps))
+    warmup = max(1, min(args.warmup, 5))
+    v, cores, wall = cpu_sample(cfg, steps=steps, warmup=warmup)
     line = {
         "impl": "reference", "metric": "interior voxel-steps/s", "value": v, "unit": "voxel-steps/s",
-        "n_gpus": world, "steps": steps, "warmup": min(args.warmup, 2), "ms_per_step": wall / steps * 1e3,
+        "n_gpus": world, "steps": steps, "warmup": warmup, "ms_per_step": wall / steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": desc},
         "cpu_baseline": {"value": v, "unit": "voxel-steps/s", "cores": cores, "kind": "port",
-                         "sample": f"{steps} pulse steps of the workload (deposition + sweep) after 2 untimed, "
-                                   "FP64 oracle (C/OpenMP restatement of the reference kernels)"},
+                         "sample": f"{steps} pulse steps of the workload (deposition + sweep) after {warmup} untimed, "
+                                   f"FP64 oracle (C/OpenMP restatement of the reference kernels), {wall:.1f} s timed"},
         "e2e": {"value": v, "unit": "voxel-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -381,9 +384,9 @@ def run_gb300(args):
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        v, cores, wall = cpu_sample(cfg, steps=args.ref_steps)
+        v, cores, wall = cpu_sample(cfg, steps=args.cpu_steps)
         cpu = {"value": v, "unit": "voxel-steps/s", "cores": cores, "kind": "port",
-               "sample": f"{args.ref_steps} pulse steps of the same workload after 2 untimed (page first-touch), "
+               "sample": f"{args.cpu_steps} pulse steps of the same workload after 2 untimed (page first-touch), "
                          f"FP64 oracle, {wall:.1f} s timed"}
 
     if rank == 0:
@@ -425,7 +428,10 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["saturation_sweep", "adjoint"], default="full_electrode_5um")
     ap.add_argument("--dtype", choices=["float32", "float64"], default="float32")
     ap.add_argument("--e2e-steps", type=int, default=600)
-    ap.add_argument("--ref-steps", type=int, default=3)
+    ap.add_argument("--cpu-steps", dest="cpu_steps", type=int, default=50,
+                    help="pulse steps of the float64 oracle timed for the cpu_baseline (~0.2 s each at full size)")
+    ap.add_argument("--ref-max-steps", dest="ref_max_steps", type=int, default=300,
+                    help="--impl reference: at most this many timed steps")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--sweep-configs", dest="sweep_configs", type=int, default=64,
                     help="saturation_sweep: run the first N of the 64 configurations (profiling-size cases)")
