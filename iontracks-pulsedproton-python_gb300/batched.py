@@ -2,7 +2,8 @@
 
 ``run_batched_b200(configs)`` returns one reference :class:`Result` per
 configuration -- the same results ``run_simulation_b200`` gives for each of
-them alone -- but advances all grids together: each global step is one
+them alone -- but advances all grids together (the track centres drawn on the
+host one chunk of global steps ahead of the device, feeder.py): each global step is one
 deposition launch over the step's tracks of every grid and one fused-step
 launch over every active grid (``pic_batched_segment``). The grids may differ
 in every respect: size, voltage and gap (hence time step and coefficients),
@@ -27,6 +28,7 @@ import numpy as np
 from . import _native as N
 from .config import SimulationConfig
 from .engine import make_grid
+from .feeder import TrackFeeder
 from .pulses import TrackSampler, build_track_schedule
 from .state import Diagnostics, collection_efficiency
 
@@ -161,19 +163,19 @@ def run_batched_b200(
     grids = [make_grid(c, dtype, alpha_cm3_s) for c in configs]
     totals = [int(c.total_time_steps) for c in configs]
 
-    # --- tracks of every grid, sampled on the host (same stream as the reference)
+    # --- schedules of every grid, drawn on the host (same stream as the
+    # reference); the track centres are drawn later, chunk by chunk, while the
+    # device runs the previous chunk (feeder.py)
     rngs = rngs if rngs is not None else [np.random.default_rng(c.seed) for c in configs]
-    xs_parts, ys_parts, offsets = [], [], []
+    offsets, samplers = [], []
     track_base = []
     base = 0
     for c, rng in zip(configs, rngs):
         sched = build_track_schedule(c, rng)
         n_tr = int(sched.sum())
-        xs, ys = TrackSampler(rng, c.mid_xy, c.sampling_radius, c.no_xy).sample(n_tr)
+        samplers.append(TrackSampler(rng, c.mid_xy, c.sampling_radius, c.no_xy))
         off = np.zeros(len(sched) + 1, dtype=np.int64)
         np.cumsum(sched, out=off[1:])
-        xs_parts.append(xs)
-        ys_parts.append(ys)
         offsets.append(off)
         track_base.append(base)
         base += n_tr
@@ -212,8 +214,8 @@ def run_batched_b200(
     dens = [torch.zeros(max(2 * do, 2), dtype=tdt, **kw) for _ in range(2)]  # deposition pairs
     counts = torch.zeros(max(co, 1), dtype=torch.int32, **kw)
     tally = torch.zeros((max(to, 1), 4), dtype=torch.float64, **kw)
-    xs_dev = torch.from_numpy(np.concatenate(xs_parts) if base else np.zeros(1)).to(dev)
-    ys_dev = torch.from_numpy(np.concatenate(ys_parts) if base else np.zeros(1)).to(dev)
+    xs_dev = torch.zeros(max(base, 1), dtype=torch.float64, device=dev)
+    ys_dev = torch.zeros(max(base, 1), dtype=torch.float64, device=dev)
 
     # --- per global step: tasks (grid, first track, first warp), in grid
     # order within a step; M[s, c] = tracks of grid c at global step s
@@ -269,11 +271,25 @@ def run_batched_b200(
     workspace = torch.zeros(int(wsb.value), dtype=torch.uint8, device=dev)
 
     st = torch.cuda.current_stream(dev).cuda_stream
+    # chunks of global steps; chunk (c0, c1) needs grid c's tracks
+    # [offsets[c][min(c0, T_c)], offsets[c][min(c1, T_c)])
+    chunks = [(c0, min(c0 + chunk_steps, s1), tab) for s0, s1, tab in phases for c0 in range(s0, s1, chunk_steps)]
+
+    def jobs_of(c0, c1):
+        out = []
+        for c in range(n_cfg):
+            a, b = offsets[c][min(c0, totals[c])], offsets[c][min(c1, totals[c])]
+            out.append((samplers[c], int(b - a), int(track_base[c] + a)))
+        return out
+
+    feeder = TrackFeeder(torch, dev, max((sum(n for _, n, _ in jobs_of(c0, c1)) for c0, c1, _ in chunks), default=1))
     t0 = perf_counter()
-    for s0, s1, tab in phases:
-        c0 = s0
-        while c0 < s1:
-            c1 = min(c0 + chunk_steps, s1)
+    try:
+        pending = feeder.submit(jobs_of(*chunks[0][:2])) if chunks else None
+        for k, (c0, c1, tab) in enumerate(chunks):
+            feeder.upload(pending, xs_dev, ys_dev)
+            # draw the next chunk's tracks while the device runs this one
+            pending = feeder.submit(jobs_of(*chunks[k + 1][:2])) if k + 1 < len(chunks) else None
             L = PicBatchLaunch()
             L.cfgs = cfg_dev.data_ptr()
             L.n_cfgs = n_cfg
@@ -300,8 +316,9 @@ def run_batched_b200(
             N.check(lib.pic_batched_segment(ctypes.byref(L), st), "pic_batched_segment")
             if progress:
                 print(f"  global step {c1}/{S}")
-            c0 = c1
-    torch.cuda.synchronize(dev)
+        torch.cuda.synchronize(dev)
+    finally:
+        feeder.close()
     elapsed = perf_counter() - t0
 
     # --- one Result per configuration

@@ -130,11 +130,22 @@ class TrackSampler:
         n_tracks = int(n_tracks)
         if n_tracks <= 0:
             return np.empty(0), np.empty(0)
+        return self.sample_into(np.empty(n_tracks), np.empty(n_tracks))
+
+    def sample_into(self, xs_out: np.ndarray, ys_out: np.ndarray):
+        """Fill the contiguous float64 arrays ``xs_out``/``ys_out`` (equal
+        lengths) with the next accepted centres -- e.g. views of pinned
+        staging memory -- and return them."""
+        n_tracks = len(xs_out)
+        if len(ys_out) != n_tracks or xs_out.dtype != np.float64 or ys_out.dtype != np.float64:
+            raise ValueError("xs_out and ys_out must be float64 arrays of equal length")
+        if not (xs_out.flags.c_contiguous and ys_out.flags.c_contiguous):
+            raise ValueError("xs_out and ys_out must be contiguous")
+        if n_tracks == 0:
+            return xs_out, ys_out
         if self._pcg64:
-            return self._sample_pcg64(n_tracks)
+            return self._sample_pcg64(n_tracks, xs_out, ys_out)
         lib = N.load()
-        xs_out = np.empty(n_tracks)
-        ys_out = np.empty(n_tracks)
         acc, used = ctypes.c_int64(), ctypes.c_int64()
         filled = 0
         while filled < n_tracks:
@@ -153,15 +164,13 @@ class TrackSampler:
                 self._pos = 0
         return xs_out, ys_out
 
-    def _sample_pcg64(self, n_tracks: int):
+    def _sample_pcg64(self, n_tracks: int, xs_out: np.ndarray, ys_out: np.ndarray):
         """Draw and scan in one native pass (``pic_sample_disc_pcg64``) from
         the generator's PCG64 state, then store the advanced state back: the
         generator ends exactly past the doubles consumed, so the next call
         (or any later draw) continues the stream."""
         lib = N.load()
         d, st = _pcg64_state(self.rng)
-        xs_out = np.empty(n_tracks)
-        ys_out = np.empty(n_tracks)
         acc, draws = ctypes.c_int64(), ctypes.c_int64()
         filled = 0
         while filled < n_tracks:

@@ -9,8 +9,10 @@ it drops in beside them and under the reference's output writers.
 How a run is driven:
 
 * the schedule and the track centres are drawn on the host from the same
-  NumPy stream as the reference (identical tracks for the same seed); a whole
-  pulse is sampled in one call and uploaded in one copy;
+  NumPy stream as the reference (identical tracks for the same seed), one
+  chunk of steps at a time on a worker thread: the next chunk's tracks are
+  drawn while the device runs the current one, and copied into the pulse's
+  device track buffer just before the steps that read them;
 * each pulse is one segment of steps on the device (deposition + fused step
   per time step), the clearance gaps are segments without deposition; the
   library's host loop launches a segment's kernels back to back with no host
@@ -32,6 +34,7 @@ from typing import Optional
 import numpy as np
 
 from .engine import ChamberEngine
+from .feeder import TrackFeeder
 from .pulses import TrackSampler, build_track_schedule
 from .state import Diagnostics, collection_efficiency
 
@@ -108,23 +111,36 @@ def run_simulation_b200(
     report_every = max(1, total // 20)
     loop_t0 = perf_counter()
     steps_done = 0
-    stopped = False
 
+    # The run as chunks of at most chunk_steps steps (within a pulse or an
+    # idle stretch). Chunks bound the wall-clock check and the progress
+    # report; the device never waits on the host inside a chunk. A chunk's
+    # tracks occupy [t0, t1) of the pulse's device track buffer.
+    units = []
     for s0, s1, with_tracks in _segments(config, last_step):
+        offsets = np.zeros(s1 - s0 + 1, dtype=np.int64)
         if with_tracks:
-            counts = schedule[s0:s1]
-            n = int(counts.sum())
-            xs, ys = sampler.sample(n)
-            eng.upload_tracks(xs, ys)
-            offsets = np.zeros(len(counts) + 1, dtype=np.int64)
-            np.cumsum(counts, out=offsets[1:])
-        else:
-            offsets = np.zeros(s1 - s0 + 1, dtype=np.int64)
-        # Chunks bound the wall-clock check and the progress report; the
-        # device never waits on the host inside a chunk.
-        c0 = 0
-        while c0 < s1 - s0:
+            np.cumsum(schedule[s0:s1], out=offsets[1:])
+        for c0 in range(0, s1 - s0, chunk_steps):
             c1 = min(c0 + chunk_steps, s1 - s0)
+            units.append((s0, with_tracks, c0, c1, offsets))
+    feeds = [u for u, (_, wt, c0, c1, off) in enumerate(units) if wt and off[c1] > off[c0]]
+    feeder = TrackFeeder(torch, eng.device, max((int(units[u][4][units[u][3]] - units[u][4][units[u][2]])
+                                                  for u in feeds), default=1))
+
+    def submit(k):  # draw the tracks of the k-th chunk with tracks
+        s0, _, c0, c1, off = units[feeds[k]]
+        return feeder.submit([(sampler, off[c1] - off[c0], off[c0])])
+
+    try:
+        pending = submit(0) if feeds else None
+        next_feed = 0
+        for u, (s0, with_tracks, c0, c1, offsets) in enumerate(units):
+            if next_feed < len(feeds) and feeds[next_feed] == u:
+                feeder.upload(pending, eng.xs, eng.ys)
+                next_feed += 1
+                # draw the next chunk's tracks while the device runs this one
+                pending = submit(next_feed) if next_feed < len(feeds) else None
             seg = offsets[c0 : c1 + 1] - offsets[c0]
             if use_graphs:
                 # the same chunk of every pulse (or of every idle stretch) has
@@ -139,13 +155,10 @@ def run_simulation_b200(
             if max_wall_s is not None:
                 torch.cuda.synchronize(eng.device)
                 if perf_counter() - loop_t0 >= max_wall_s:
-                    stopped = True
                     break
-            c0 = c1
-        if stopped:
-            break
-
-    torch.cuda.synchronize(eng.device)
+        torch.cuda.synchronize(eng.device)
+    finally:
+        feeder.close()
     loop_elapsed_s = perf_counter() - loop_t0
     eng.check_status()
     tallies = eng.tallies(steps_done)
