@@ -383,6 +383,19 @@ int pic_batched_segment(const pic_batch_launch *launch, uintptr_t stream);
  * pic_graph_launch, free with pic_graph_destroy). */
 int pic_batched_graph_create(const pic_batch_launch *launch, uintptr_t stream, uintptr_t *graph_out);
 
+/* The same global steps in ONE persistent launch (a cooperative launch, one
+ * block per resident slot): per step the deposition of every grid's tracks
+ * and the fused step over the work table, separated by device-wide barriers
+ * whose waits are bounded. step_task_off_dev / step_tracks_dev are device
+ * copies of the step tables indexed by GLOBAL step (launch->step_task_off /
+ * step_tracks, the host copies for this chunk, are still required: they are
+ * validated). After the run, pic_batched_status reads the status word: 0, or
+ * 5 when a barrier wait gave up after its bounded polls (the results are then
+ * invalid). The workspace is pic_batched_workspace_bytes, zeroed once. */
+int pic_batched_persistent(const pic_batch_launch *launch, const int64_t *step_task_off_dev,
+                           const int64_t *step_tracks_dev, uintptr_t stream);
+int pic_batched_status(const pic_batch_launch *launch, uintptr_t stream, int32_t *status);
+
 #ifdef __cplusplus
 }
 #endif

@@ -129,6 +129,8 @@ EXPORTS = {
          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
          ctypes.c_int64, ctypes.c_void_p],
     ),
+    "pic_batched_persistent": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "pic_batched_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]),
     "pic_capture_begin": (ctypes.c_int, [ctypes.c_void_p]),
     "pic_capture_end": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
     "pic_run_segment": (

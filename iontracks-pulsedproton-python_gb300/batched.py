@@ -142,11 +142,18 @@ def run_batched_b200(
     alpha_cm3_s: Optional[float] = None,
     chunk_steps: int = 512,
     progress: bool = False,
+    persistent: bool = False,
 ):
     """Simulate every configuration and return their Results, in order.
 
     Equivalent to ``[run_simulation_b200(c) for c in configs]`` (same tracks,
     same tallies to float32 rounding) but with all grids advanced together.
+    ``persistent`` runs each chunk of ``chunk_steps`` global steps as one
+    persistent launch (``pic_batched_persistent``: deposition and step phases
+    separated by device-wide barriers); otherwise (the default) each global
+    step is two launches (``pic_batched_segment``). Measured on GB300 over the
+    64-configuration sweep the per-step launches are faster (1.31 vs 1.44 s):
+    two device-wide barriers per step cost what two launch gaps do.
     """
     import torch
 
@@ -271,6 +278,8 @@ def run_batched_b200(
     workspace = torch.zeros(int(wsb.value), dtype=torch.uint8, device=dev)
 
     st = torch.cuda.current_stream(dev).cuda_stream
+    sto_dev = torch.from_numpy(step_task_off).to(dev)
+    stt_dev = torch.from_numpy(np.ascontiguousarray(step_tracks, dtype=np.int64)).to(dev)
     # chunks of global steps; chunk (c0, c1) needs grid c's tracks
     # [offsets[c][min(c0, T_c)], offsets[c][min(c1, T_c)])
     chunks = [(c0, min(c0 + chunk_steps, s1), tab) for s0, s1, tab in phases for c0 in range(s0, s1, chunk_steps)]
@@ -313,10 +322,20 @@ def run_batched_b200(
             L.first_step, L.n_steps = c0, c1 - c0
             L.counts, L.tally = counts.data_ptr(), tally.data_ptr()
             L.workspace, L.workspace_bytes = workspace.data_ptr(), workspace.numel()
-            N.check(lib.pic_batched_segment(ctypes.byref(L), st), "pic_batched_segment")
+            if persistent:
+                N.check(lib.pic_batched_persistent(ctypes.byref(L), sto_dev.data_ptr(), stt_dev.data_ptr(), st),
+                        "pic_batched_persistent")
+            else:
+                N.check(lib.pic_batched_segment(ctypes.byref(L), st), "pic_batched_segment")
             if progress:
                 print(f"  global step {c1}/{S}")
         torch.cuda.synchronize(dev)
+        if persistent and chunks:
+            status = ctypes.c_int32()
+            N.check(lib.pic_batched_status(ctypes.byref(L), st, ctypes.byref(status)), "pic_batched_status")
+            if status.value != 0:
+                raise RuntimeError(f"the persistent batched kernel gave up on a barrier (status {status.value}); "
+                                   "results are invalid")
     finally:
         feeder.close()
     elapsed = perf_counter() - t0

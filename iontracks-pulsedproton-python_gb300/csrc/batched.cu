@@ -89,15 +89,13 @@ __device__ __forceinline__ void red_load_add(DF &acc, const double *slot) {
 __device__ __forceinline__ double red_of(const Tally<double> &t) { return t.value(); }
 __device__ __forceinline__ DF red_of(const Tally<float> &t) { return df_of(t); }
 
-template <typename T, int BLOCK, typename I>
-__global__ void __launch_bounds__(BLOCK) batched_step_kernel(BatchStepArgs<T> b) {
+// One entry of the work table (blk): a range of one grid's items, its
+// tallies reduced per block and, by the grid's last block to finish, into the
+// grid's tally row. `red`, `last` and `a` are the caller's shared memory.
+template <typename T, int BLOCK, typename I, bool COH = false>
+__device__ __forceinline__ void batched_step_block(const BatchStepArgs<T> &b, int blk,
+                                                   typename RedT<T>::type (*red)[4], bool &last, StepArgs<T> &a) {
     using R = typename RedT<T>::type;
-    __shared__ R red[BLOCK / 32][4];
-    __shared__ bool last;
-    // the block's grid arguments, staged once in shared memory and read by
-    // broadcast (keeps them out of the registers of every thread)
-    __shared__ StepArgs<T> a;
-    const int blk = blockIdx.x;
     const int c = b.blk_cfg[blk];
     const pic_batch_cfg &C = b.cfgs[c];
     if (threadIdx.x == 0) grid_args(C, b, a);
@@ -105,7 +103,7 @@ __global__ void __launch_bounds__(BLOCK) batched_step_kernel(BatchStepArgs<T> b)
     Tally<T> t_rec, t_p, t_n, t_inj;
     const I i1 = (I)b.blk_item1[blk];
     for (I item = (I)b.blk_item0[blk] + threadIdx.x; item < i1; item += BLOCK)
-        flat_item<T, I>(a, item, t_rec, t_p, t_n, t_inj);
+        flat_item<T, I, COH>(a, item, t_rec, t_p, t_n, t_inj);
     R v[4] = {red_of(t_inj), red_of(t_rec), red_of(t_p), red_of(t_n)};
     block_sum4<BLOCK>(v, red);
     if (threadIdx.x == 0) {
@@ -134,6 +132,35 @@ __global__ void __launch_bounds__(BLOCK) batched_step_kernel(BatchStepArgs<T> b)
     }
 }
 
+template <typename T, int BLOCK, typename I>
+__global__ void __launch_bounds__(BLOCK) batched_step_kernel(BatchStepArgs<T> b) {
+    __shared__ typename RedT<T>::type red[BLOCK / 32][4];
+    __shared__ bool last;
+    // the block's grid arguments, staged once in shared memory and read by
+    // broadcast (keeps them out of the registers of every thread)
+    __shared__ StepArgs<T> a;
+    batched_step_block<T, BLOCK, I>(b, blockIdx.x, red, last, a);
+}
+
+// Warp w of a global step's deposition: the track it owns, found in the
+// step's task list (grid, first track, first warp) by binary search.
+template <typename T>
+__device__ __forceinline__ void batched_deposit_warp(const pic_batch_cfg *cfgs, const int32_t *task_cfg,
+                                                     const int64_t *task_first, const int64_t *task_prefix,
+                                                     int n_tasks, int64_t w, const double *xs, const double *ys,
+                                                     pair_t<T> *dens, uint32_t *counts, int lane) {
+    int lo = 0, hi = n_tasks - 1;  // last task whose first warp is <= w
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (task_prefix[mid] <= w) lo = mid; else hi = mid - 1;
+    }
+    const pic_batch_cfg &C = cfgs[task_cfg[lo]];
+    const int64_t idx = task_first[lo] + (w - task_prefix[lo]);
+    const int64_t n = C.grid.no_xy;
+    deposit_track<T>(xs[idx], ys[idx], n, (n + 3) / 4 * 4, C.grid.cutoff_voxels, (T)C.grid.h2_over_b2,
+                     (T)C.grid.gaussian_factor, dens + C.dens_off, counts + C.counts_off, lane);
+}
+
 template <typename T, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) batched_deposit_kernel(const pic_batch_cfg *cfgs,
                                                                       const int32_t *task_cfg,
@@ -144,28 +171,181 @@ __global__ void __launch_bounds__(WARPS * 32) batched_deposit_kernel(const pic_b
                                                                       uint32_t *counts) {
     const int64_t w = (int64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
     if (w >= total) return;
-    // last task whose first warp is <= w
-    int lo = 0, hi = n_tasks - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (task_prefix[mid] <= w) lo = mid; else hi = mid - 1;
-    }
-    const pic_batch_cfg &C = cfgs[task_cfg[lo]];
-    const int64_t idx = task_first[lo] + (w - task_prefix[lo]);
-    const int64_t n = C.grid.no_xy;
-    deposit_track<T>(xs[idx], ys[idx], n, (n + 3) / 4 * 4, C.grid.cutoff_voxels, (T)C.grid.h2_over_b2,
-                     (T)C.grid.gaussian_factor, dens + C.dens_off, counts + C.counts_off, threadIdx.x & 31);
+    batched_deposit_warp<T>(cfgs, task_cfg, task_first, task_prefix, n_tasks, w, xs, ys, dens, counts,
+                            threadIdx.x & 31);
 }
 
 // Workspace layout: [per-grid completion counters, n_cfgs x u32, padded to
-// 256 bytes | per-block partials, n_blocks x 4 doubles]. The counters sit at a
-// fixed place whatever the block count of a launch (which changes when grids
-// finish), so they stay zero between steps.
+// 256 bytes | the persistent kernel's barrier and status, 256 bytes |
+// per-block partials, n_blocks x 4 doubles]. The counters sit at a fixed place
+// whatever the block count of a launch (which changes when grids finish), so
+// they stay zero between steps.
 static int64_t counters_bytes(int32_t n_cfgs) { return ((int64_t)n_cfgs * 4 + 255) / 256 * 256; }
+constexpr int64_t kBarrierBytes = 256;
+
+struct GridBarrier {
+    unsigned int count;  // blocks arrived at the current barrier
+    unsigned int gen;    // barriers completed
+    int status;          // 0, or the code of a wait that gave up
+};
+
+static GridBarrier *barrier_of(const BatchLaunch &L) {
+    return reinterpret_cast<GridBarrier *>(static_cast<char *>(L.workspace) + counters_bytes(L.n_cfgs));
+}
+static double *partials_of(const BatchLaunch &L) {
+    return reinterpret_cast<double *>(static_cast<char *>(L.workspace) + counters_bytes(L.n_cfgs) + kBarrierBytes);
+}
 
 int batched_workspace_bytes(int32_t n_blocks, int32_t n_cfgs, int64_t *bytes) {
     if (n_blocks < 1 || n_cfgs < 1) return set_error(PIC_E_INVALID, "n_blocks and n_cfgs must be >= 1");
-    *bytes = counters_bytes(n_cfgs) + (int64_t)n_blocks * 4 * 8;
+    *bytes = counters_bytes(n_cfgs) + kBarrierBytes + (int64_t)n_blocks * 4 * 8;
+    return PIC_OK;
+}
+
+// Device-wide barrier of a cooperative launch (every block resident). The
+// last block to arrive resets the count and opens the barrier; the others wait
+// for that, a bounded number of polls: a wait that runs out sets the status
+// word and every block leaves at its next barrier (the host then reads the
+// status). Returns false when the kernel must stop.
+constexpr long long kBarrierPolls = 1LL << 24;  // x ~100 ns: a few seconds
+
+__device__ bool grid_barrier(GridBarrier *bar) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile GridBarrier *vb = bar;
+        const unsigned int g = vb->gen;
+        __threadfence();  // this block's writes before its arrival
+        ok = 1;
+        if (atomicAdd(&bar->count, 1u) == gridDim.x - 1) {
+            atomicExch(&bar->count, 0u);
+            __threadfence();
+            atomicAdd(&bar->gen, 1u);
+        } else {
+            long long polls = 0;
+            while (vb->gen == g) {
+                if (vb->status != 0) {
+                    ok = 0;
+                    break;
+                }
+                if (++polls > kBarrierPolls) {
+                    atomicCAS(&bar->status, 0, 5);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(100);
+            }
+        }
+        __threadfence();  // the other blocks' writes before this block reads
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+template <typename T>
+struct BatchPersistArgs {
+    BatchStepArgs<T> b;  // step and parity fields set per step
+    const void *pos[2], *neg[2], *dens[2];
+    const int32_t *task_cfg;
+    const int64_t *task_first, *task_prefix;
+    const int64_t *step_task_off, *step_tracks;  // device, by global step
+    const double *xs, *ys;
+    uint32_t *counts;
+    int n_blocks;
+    int64_t first_step, n_steps;
+    GridBarrier *bar;
+};
+
+// A chunk of global steps in one launch: per step, the deposition of every
+// grid's tracks (warps over the step's tracks), a barrier, the fused step over
+// the work table (blocks loop over its entries), a barrier.
+template <typename T, typename I>
+__global__ void __launch_bounds__(256) batched_persistent_kernel(BatchPersistArgs<T> p) {
+    constexpr int BLOCK = 256, WARPS = BLOCK / 32;
+    __shared__ typename RedT<T>::type red[BLOCK / 32][4];
+    __shared__ bool last;
+    __shared__ StepArgs<T> a;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int64_t s = p.first_step; s < p.first_step + p.n_steps; ++s) {
+        const int bi = (int)(s & 1), bo = bi ^ 1;
+        const int64_t t0 = p.step_task_off[s], t1 = p.step_task_off[s + 1], tracks = p.step_tracks[s];
+        if (tracks > 0 && t1 > t0) {
+            for (int64_t w = (int64_t)blockIdx.x * WARPS + warp; w < tracks; w += (int64_t)gridDim.x * WARPS)
+                batched_deposit_warp<T>(p.b.cfgs, p.task_cfg + t0, p.task_first + t0, p.task_prefix + t0,
+                                        (int)(t1 - t0), w, p.xs, p.ys, (pair_t<T> *)p.dens[bi], p.counts, lane);
+            if (!grid_barrier(p.bar)) return;
+        }
+        BatchStepArgs<T> b = p.b;
+        b.pos_in = (const T *)p.pos[bi];
+        b.neg_in = (const T *)p.neg[bi];
+        b.pos_out = (T *)p.pos[bo];
+        b.neg_out = (T *)p.neg[bo];
+        b.dens = (const pair_t<T> *)p.dens[bi];
+        b.dens_zero = (pair_t<T> *)p.dens[bo];
+        b.step = s;
+        for (int vb = blockIdx.x; vb < p.n_blocks; vb += gridDim.x) {
+            __syncthreads();  // shared staging of the previous entry is done with
+            batched_step_block<T, BLOCK, I, true>(b, vb, red, last, a);
+        }
+        if (!grid_barrier(p.bar)) return;
+    }
+}
+
+template <typename T, typename I>
+static int launch_persistent(const BatchLaunch &L, const int64_t *sto, const int64_t *stt, cudaStream_t st) {
+    static int per_sm = 0;  // resident blocks per SM of this instantiation
+    if (per_sm == 0) {
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_persistent_kernel<T, I>, 256, 0);
+        if (e != cudaSuccess || per_sm < 1) {
+            per_sm = 0;
+            return set_cuda_error("cudaOccupancyMaxActiveBlocksPerMultiprocessor(batched_persistent_kernel)", e);
+        }
+    }
+    BatchPersistArgs<T> p;
+    p.b = BatchStepArgs<T>{L.cfgs, L.blk_cfg, L.blk_item0, L.blk_item1, L.cfg_blk0, L.cfg_nblk, nullptr, nullptr,
+                           nullptr, nullptr, nullptr, nullptr, L.tally, partials_of(L),
+                           reinterpret_cast<unsigned int *>(L.workspace), 0};
+    for (int q = 0; q < 2; ++q) {
+        p.pos[q] = L.pos[q];
+        p.neg[q] = L.neg[q];
+        p.dens[q] = L.dens[q];
+    }
+    p.task_cfg = L.task_cfg;
+    p.task_first = L.task_first;
+    p.task_prefix = L.task_prefix;
+    p.step_task_off = sto;
+    p.step_tracks = stt;
+    p.xs = L.xs;
+    p.ys = L.ys;
+    p.counts = L.counts;
+    p.n_blocks = L.n_blocks;
+    p.first_step = L.first_step;
+    p.n_steps = L.n_steps;
+    p.bar = barrier_of(L);
+    cudaError_t e = cudaMemsetAsync(p.bar, 0, sizeof(GridBarrier), st);
+    if (e != cudaSuccess) return set_cuda_error("cudaMemsetAsync(barrier)", e);
+    const unsigned grid = (unsigned)(per_sm * sm_count());
+    void *args[] = {&p};
+    e = cudaLaunchCooperativeKernel((const void *)batched_persistent_kernel<T, I>, dim3(grid), dim3(256), args, 0, st);
+    if (e != cudaSuccess) return set_cuda_error("cudaLaunchCooperativeKernel(batched_persistent_kernel)", e);
+    return PIC_OK;
+}
+
+int batched_persistent(const BatchLaunch &L, const int64_t *step_task_off, const int64_t *step_tracks,
+                       cudaStream_t st) {
+    if (L.dtype == PIC_F64)
+        return L.index32 ? launch_persistent<double, uint32_t>(L, step_task_off, step_tracks, st)
+                         : launch_persistent<double, int64_t>(L, step_task_off, step_tracks, st);
+    return L.index32 ? launch_persistent<float, uint32_t>(L, step_task_off, step_tracks, st)
+                     : launch_persistent<float, int64_t>(L, step_task_off, step_tracks, st);
+}
+
+int batched_status(const BatchLaunch &L, cudaStream_t st, int32_t *status) {
+    int v = 0;
+    cudaError_t e = cudaMemcpyAsync(&v, &barrier_of(L)->status, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return set_cuda_error("reading the batched status word", e);
+    *status = v;
     return PIC_OK;
 }
 
@@ -182,7 +362,7 @@ static void launch_batched_step(const BatchLaunch &L, int bi, int bo, double *pa
 int batched_loop(const BatchLaunch &L, cudaStream_t st) {
     constexpr int WARPS = 8;
     unsigned int *counters = reinterpret_cast<unsigned int *>(L.workspace);
-    double *partials = reinterpret_cast<double *>(reinterpret_cast<char *>(L.workspace) + counters_bytes(L.n_cfgs));
+    double *partials = partials_of(L);
     for (int64_t s = 0; s < L.n_steps; ++s) {
         const int64_t step = L.first_step + s;
         const int bi = (int)(step & 1), bo = bi ^ 1;

@@ -593,6 +593,20 @@ int pic_batched_segment(const pic_batch_launch *launch, uintptr_t stream) {
     return batched_loop(*launch, reinterpret_cast<cudaStream_t>(stream));
 }
 
+int pic_batched_persistent(const pic_batch_launch *launch, const int64_t *step_task_off_dev,
+                           const int64_t *step_tracks_dev, uintptr_t stream) {
+    int rc = check_batch(launch);  // validates the host copies of the step tables
+    if (rc) return rc;
+    if (!step_task_off_dev || !step_tracks_dev) return set_error(PIC_E_INVALID, "device step tables are null");
+    if (launch->n_steps == 0) return PIC_OK;
+    return batched_persistent(*launch, step_task_off_dev, step_tracks_dev, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int pic_batched_status(const pic_batch_launch *launch, uintptr_t stream, int32_t *status) {
+    if (!launch || !launch->workspace || !status) return set_error(PIC_E_INVALID, "null pointer argument");
+    return batched_status(*launch, reinterpret_cast<cudaStream_t>(stream), status);
+}
+
 int pic_batched_graph_create(const pic_batch_launch *launch, uintptr_t stream, uintptr_t *graph_out) {
     if (!graph_out) return set_error(PIC_E_INVALID, "graph_out is null");
     *graph_out = 0;

@@ -29,6 +29,18 @@ __device__ __forceinline__ V4<double> load4(const double *p) {
     double2 b = __ldg(reinterpret_cast<const double2 *>(p) + 1);
     return {{a.x, a.y, b.x, b.y}};
 }
+// Coherent forms (plain global loads) for kernels that read data written
+// earlier in the same launch by other blocks (the persistent batched kernel):
+// the read-only path of __ldg is not kept coherent with such writes.
+__device__ __forceinline__ V4<float> load4c(const float *p) {
+    const float4 t = *reinterpret_cast<const float4 *>(p);
+    return {{t.x, t.y, t.z, t.w}};
+}
+__device__ __forceinline__ V4<double> load4c(const double *p) {
+    const double2 a = reinterpret_cast<const double2 *>(p)[0];
+    const double2 b = reinterpret_cast<const double2 *>(p)[1];
+    return {{a.x, a.y, b.x, b.y}};
+}
 __device__ __forceinline__ void store4(float *p, const V4<float> &v) {
     *reinterpret_cast<float4 *>(p) = make_float4(v.v[0], v.v[1], v.v[2], v.v[3]);
 }

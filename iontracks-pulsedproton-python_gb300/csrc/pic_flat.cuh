@@ -54,10 +54,13 @@ __device__ __forceinline__ bool scored_col_t(const ScoreTest &t, I i, I j) {
 // The fused step for one work item: four consecutive k of output column
 // (i, j), decoded from the flat item index (k-vector fastest). Adds the
 // item's scored contributions to the thread's running tallies. I is the index
-// type (uint32_t when flat_index32 holds for the grid, else int64_t).
-template <typename T, typename I>
+// type (uint32_t when flat_index32 holds for the grid, else int64_t). COH:
+// plain (coherent) vector loads instead of the read-only path, for a kernel
+// that reads fields other blocks wrote earlier in the same launch.
+template <typename T, typename I, bool COH = false>
 __device__ __forceinline__ void flat_item(const StepArgs<T> &a, I item, Tally<T> &t_rec,
                                           Tally<T> &t_p, Tally<T> &t_n, Tally<T> &t_inj) {
+    auto ld4 = [](const T *p) { return COH ? load4c(p) : load4(p); };
     const I n = (I)a.n, kp = (I)a.kp, c4 = (I)a.c4, dp = (I)a.dp;
     const I col = item / c4;
     const int c = (int)(item - col * c4);
@@ -79,7 +82,7 @@ __device__ __forceinline__ void flat_item(const StepArgs<T> &a, I item, Tally<T>
 
     if (ring && !a.reflecting) {
         const T d = dep_at(a, (int64_t)(i * dp + j));
-        V4<T> P = load4(a.pos_in + out_off), N = load4(a.neg_in + out_off);
+        V4<T> P = ld4(a.pos_in + out_off), N = ld4(a.neg_in + out_off);
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
             P.v[e] += g[e] ? d : T(0);
@@ -93,11 +96,11 @@ __device__ __forceinline__ void flat_item(const StepArgs<T> &a, I item, Tally<T>
     const I ccol = ci * n + cj;
     const I base = ccol * kp + k0;
     const I di = n * kp;
-    V4<T> P = load4(a.pos_in + base), N = load4(a.neg_in + base);
-    V4<T> Pim = load4(a.pos_in + base - di), Pip = load4(a.pos_in + base + di);
-    V4<T> Pjm = load4(a.pos_in + base - kp), Pjp = load4(a.pos_in + base + kp);
-    V4<T> Nim = load4(a.neg_in + base - di), Nip = load4(a.neg_in + base + di);
-    V4<T> Njm = load4(a.neg_in + base - kp), Njp = load4(a.neg_in + base + kp);
+    V4<T> P = ld4(a.pos_in + base), N = ld4(a.neg_in + base);
+    V4<T> Pim = ld4(a.pos_in + base - di), Pip = ld4(a.pos_in + base + di);
+    V4<T> Pjm = ld4(a.pos_in + base - kp), Pjp = ld4(a.pos_in + base + kp);
+    V4<T> Nim = ld4(a.neg_in + base - di), Nip = ld4(a.neg_in + base + di);
+    V4<T> Njm = ld4(a.neg_in + base - kp), Njp = ld4(a.neg_in + base + kp);
     T pkm = c > 0 ? a.pos_in[base - 1] : T(0);
     T nkm = c > 0 ? a.neg_in[base - 1] : T(0);
     T pkp = k0 + 4 < kp ? a.pos_in[base + 4] : T(0);

@@ -91,6 +91,9 @@ int launch_deposit(const pic_grid *g, const double *xs, const double *ys, int64_
 using BatchLaunch = pic_batch_launch;
 int batched_workspace_bytes(int32_t n_blocks, int32_t n_cfgs, int64_t *bytes);
 int batched_loop(const BatchLaunch &L, cudaStream_t st);
+int batched_persistent(const BatchLaunch &L, const int64_t *step_task_off, const int64_t *step_tracks,
+                       cudaStream_t st);
+int batched_status(const BatchLaunch &L, cudaStream_t st, int32_t *status);
 
 int step_noalloc(const pic_grid *g, const void *pos_in, const void *neg_in, void *pos_out, void *neg_out,
                  const double *xs, const double *ys, int64_t n_tracks, uint32_t *counts, double *tally,

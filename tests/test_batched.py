@@ -91,3 +91,22 @@ def test_batched_sweep_subset_matches_the_oracle(oracle):
         ref = oracle.run(cfg, mode="batched", threads=8, keep_fields=False)
         np.testing.assert_array_equal(got.track_density_xy, ref["track_density_xy"])
         assert abs(got.ks - ref["ks"]) <= KS_ABS
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype", ["float32", "float64"])
+def test_persistent_launch_matches_per_step_launches(dtype):
+    """The persistent form (one cooperative launch per chunk of global steps,
+    device-wide barriers between the deposition and step phases) gives the
+    per-step launches' results: identical tracks, k_s and tallies to the
+    dtype's rounding; a chunk of 7 steps makes grids start and finish inside
+    launches."""
+    cfgs = _mixed_batch()
+    a = pkg().run_batched_b200(cfgs, dtype=dtype, chunk_steps=7)
+    b = pkg().run_batched_b200(cfgs, dtype=dtype, chunk_steps=7, persistent=True)
+    tol = 1e-5 if dtype == "float32" else 1e-12
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x.track_density_xy, y.track_density_xy)
+        assert abs(x.ks - y.ks) <= tol
+        np.testing.assert_allclose(y.recombination, x.recombination, rtol=0,
+                                   atol=tol * max(np.abs(x.recombination).max(), 1e-300))
