@@ -295,3 +295,26 @@ def test_full_electrode_float64_matches_the_published_ks():
     float64 rounding (measured |dk_s| = 4.4e-16)."""
     res = _solver()(_published_full_electrode_config(), progress=False, return_fields=False, dtype="float64")
     assert abs(res.ks - PUBLISHED_FULL_ELECTRODE_KS) <= 1e-12
+
+
+# The reference's published 10 um ladder (same chamber, sampled radius varied;
+# no_z_electrode = 5; 2 194 steps): (radius cm, no_xy, k_s) from
+# profiling/data/gpu_athena/ladder_10um.json -- its CPU and CUDA float64 runs
+# agree on every row.
+PUBLISHED_LADDER_10UM = [
+    (0.014, 34, 1.101078104284521),
+    (0.05, 106, 1.108750400628538),
+    (0.08, 166, 1.1098094977890123),
+    (0.12, 246, 1.1104074023012953),
+    (0.18, 366, 1.1108197003228455),
+    (0.265, 536, 1.1110811651442554),
+]
+
+
+@pytest.mark.parametrize("dtype", ["float32", "float64"])
+@pytest.mark.parametrize("radius, no_xy, ks", PUBLISHED_LADDER_10UM)
+def test_published_10um_ladder(radius, no_xy, ks, dtype):
+    cfg = make_config("aic144_full_electrode_5um", grid_size_um=10.0, sampled_radius_cm=radius, no_z_electrode=5)
+    assert (cfg.no_xy, cfg.no_z_with_buffer, cfg.total_time_steps) == (no_xy, 210, 2194)
+    res = _solver()(cfg, progress=False, return_fields=False, dtype=dtype)
+    assert abs(res.ks - ks) <= (KS_ABS if dtype == "float32" else 1e-12)
