@@ -318,3 +318,33 @@ def test_published_10um_ladder(radius, no_xy, ks, dtype):
     assert (cfg.no_xy, cfg.no_z_with_buffer, cfg.total_time_steps) == (no_xy, 210, 2194)
     res = _solver()(cfg, progress=False, return_fields=False, dtype=dtype)
     assert abs(res.ks - ks) <= (KS_ABS if dtype == "float32" else 1e-12)
+
+
+CONFIGS1 = [(dose, seed) for dose in ("column_5um_r05_d8p91", "column_5um_r05_d89p1") for seed in (1, 2, 3, 4)]
+
+
+@pytest.mark.parametrize("name, seed", CONFIGS1)
+def test_plain_method_at_scale_float32_vs_float64(name, seed):
+    """The plain method at scale: 5 um voxels, r = 0.05 cm (208 x 208 x 406,
+    3 388 steps), 8.91 and 89.1 Gy/s, seeds 1-4, one configuration per
+    launch: float32 fields within 1e-5 of the float64 fields' k_s and total
+    tallies (the float64 kernels are pinned to the oracle and to the
+    reference's published runs), identical tracks."""
+    cfg = make_config(name, seed=seed)
+    a = _solver()(cfg, progress=False, return_fields=False)
+    b = _solver()(cfg, progress=False, return_fields=False, dtype="float64")
+    np.testing.assert_array_equal(a.track_density_xy, b.track_density_xy)
+    assert abs(a.ks - b.ks) <= KS_ABS
+    assert a.recombination.sum() == pytest.approx(b.recombination.sum(), rel=TALLY_REL)
+    assert a.injected_positive.sum() == pytest.approx(b.injected_positive.sum(), rel=TALLY_REL)
+
+
+def test_plain_method_at_scale_matches_the_oracle(oracle):
+    """One of them end to end against the float64 oracle (C/OpenMP restatement
+    of the reference): 89.1 Gy/s, seed 1, 8.9 M tracks."""
+    cfg = make_config("column_5um_r05_d89p1")
+    res = _solver()(cfg, progress=False, return_fields=False)
+    ref = oracle.run(cfg, mode="batched", threads=16, keep_fields=False)
+    np.testing.assert_array_equal(res.track_density_xy, ref["track_density_xy"])
+    assert abs(res.ks - ref["ks"]) <= KS_ABS
+    assert res.recombination.sum() == pytest.approx(ref["recombined"].sum(), rel=TALLY_REL)
