@@ -26,9 +26,19 @@
 
 namespace pic {
 
+// A grid's step arguments without the buffers (filled per block from the
+// step's packed buffers and the offsets): built once per launch chunk by
+// batched_prep_kernel, copied by each block instead of recomputed.
+template <typename T>
+struct GridEntry {
+    StepArgs<T> a;
+    int64_t field_off, dens_off;
+};
+
 template <typename T>
 struct BatchStepArgs {
     const pic_batch_cfg *cfgs;
+    const GridEntry<T> *table;  // [n_cfgs]
     const int32_t *blk_cfg;
     const int64_t *blk_item0, *blk_item1;
     const int32_t *cfg_blk0, *cfg_nblk;
@@ -43,14 +53,14 @@ struct BatchStepArgs {
 };
 
 template <typename T>
-__device__ void grid_args(const pic_batch_cfg &C, const BatchStepArgs<T> &b, StepArgs<T> &a) {
+__device__ void grid_args(const pic_batch_cfg &C, StepArgs<T> &a) {
     const pic_grid &g = C.grid;
-    a.pos_in = b.pos_in + C.field_off;
-    a.neg_in = b.neg_in + C.field_off;
-    a.pos_out = b.pos_out + C.field_off;
-    a.neg_out = b.neg_out + C.field_off;
-    a.dens = b.dens + C.dens_off;
-    a.dens_zero = b.dens_zero + C.dens_off;
+    a.pos_in = a.neg_in = nullptr;
+    a.pos_out = a.neg_out = nullptr;
+    a.dens = nullptr;
+    a.dens_zero = nullptr;
+    a.tally = a.partials = nullptr;
+    a.counter = nullptr;
     a.n = g.no_xy;
     a.kp = g.kpitch;
     a.c4 = g.kpitch / 4;
@@ -68,6 +78,17 @@ __device__ void grid_args(const pic_batch_cfg &C, const BatchStepArgs<T> &b, Ste
     const double r4 = 4.0 * g.scoring_radius_sq;
     a.score.thr4 = r4 >= 4.0e18 ? (int64_t)4.0e18 : (int64_t)ceil(r4) - 1;
     a.injected_scale = (double)g.no_z;
+}
+
+template <typename T>
+__global__ void batched_prep_kernel(const pic_batch_cfg *cfgs, int n_cfgs, GridEntry<T> *table) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n_cfgs) return;
+    GridEntry<T> e;
+    grid_args(cfgs[c], e.a);
+    e.field_off = cfgs[c].field_off;
+    e.dens_off = cfgs[c].dens_off;
+    table[c] = e;
 }
 
 // Reduction type of a grid's tallies: double-float for float32 fields (no
@@ -98,7 +119,21 @@ __device__ __forceinline__ void batched_step_block(const BatchStepArgs<T> &b, in
     using R = typename RedT<T>::type;
     const int c = b.blk_cfg[blk];
     const pic_batch_cfg &C = b.cfgs[c];
-    if (threadIdx.x == 0) grid_args(C, b, a);
+    if (threadIdx.x < 32) {  // one warp copies the grid's prepared arguments
+        const GridEntry<T> *E = b.table + c;
+        const uint32_t *src = reinterpret_cast<const uint32_t *>(&E->a);
+        uint32_t *dst = reinterpret_cast<uint32_t *>(&a);
+        for (int w = threadIdx.x; w < (int)(sizeof(StepArgs<T>) / 4); w += 32) dst[w] = src[w];
+        __syncwarp();
+        if (threadIdx.x == 0) {
+            a.pos_in = b.pos_in + E->field_off;
+            a.neg_in = b.neg_in + E->field_off;
+            a.pos_out = b.pos_out + E->field_off;
+            a.neg_out = b.neg_out + E->field_off;
+            a.dens = b.dens + E->dens_off;
+            a.dens_zero = b.dens_zero + E->dens_off;
+        }
+    }
     __syncthreads();
     Tally<T> t_rec, t_p, t_n, t_inj;
     const I i1 = (I)b.blk_item1[blk];
@@ -148,7 +183,8 @@ template <typename T>
 __device__ __forceinline__ void batched_deposit_warp(const pic_batch_cfg *cfgs, const int32_t *task_cfg,
                                                      const int64_t *task_first, const int64_t *task_prefix,
                                                      int n_tasks, int64_t w, const double *xs, const double *ys,
-                                                     pair_t<T> *dens, uint32_t *counts, int lane) {
+                                                     pair_t<T> *dens, uint32_t *counts, int lane, int part,
+                                                     int nparts) {
     int lo = 0, hi = n_tasks - 1;  // last task whose first warp is <= w
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
@@ -158,7 +194,7 @@ __device__ __forceinline__ void batched_deposit_warp(const pic_batch_cfg *cfgs, 
     const int64_t idx = task_first[lo] + (w - task_prefix[lo]);
     const int64_t n = C.grid.no_xy;
     deposit_track<T>(xs[idx], ys[idx], n, (n + 3) / 4 * 4, C.grid.cutoff_voxels, (T)C.grid.h2_over_b2,
-                     (T)C.grid.gaussian_factor, dens + C.dens_off, counts + C.counts_off, lane);
+                     (T)C.grid.gaussian_factor, dens + C.dens_off, counts + C.counts_off, lane, part, nparts);
 }
 
 template <typename T, int WARPS>
@@ -168,16 +204,17 @@ __global__ void __launch_bounds__(WARPS * 32) batched_deposit_kernel(const pic_b
                                                                       const int64_t *task_prefix, int n_tasks,
                                                                       int64_t total, const double *xs,
                                                                       const double *ys, pair_t<T> *dens,
-                                                                      uint32_t *counts) {
-    const int64_t w = (int64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
-    if (w >= total) return;
-    batched_deposit_warp<T>(cfgs, task_cfg, task_first, task_prefix, n_tasks, w, xs, ys, dens, counts,
-                            threadIdx.x & 31);
+                                                                      uint32_t *counts, int parts) {
+    const int64_t w = (int64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);  // `parts` warps per track
+    if (w >= total * parts) return;
+    batched_deposit_warp<T>(cfgs, task_cfg, task_first, task_prefix, n_tasks, w / parts, xs, ys, dens, counts,
+                            threadIdx.x & 31, (int)(w % parts), parts);
 }
 
 // Workspace layout: [per-grid completion counters, n_cfgs x u32, padded to
-// 256 bytes | the persistent kernel's barrier and status, 256 bytes |
-// per-block partials, n_blocks x 4 doubles]. The counters sit at a fixed place
+// 256 bytes | the persistent kernel's barrier and status, 256 bytes | the
+// prepared grid arguments, n_cfgs slots, padded to 256 bytes | per-block
+// partials, n_blocks x 4 doubles]. The counters sit at a fixed place
 // whatever the block count of a launch (which changes when grids finish), so
 // they stay zero between steps.
 static int64_t counters_bytes(int32_t n_cfgs) { return ((int64_t)n_cfgs * 4 + 255) / 256 * 256; }
@@ -189,17 +226,34 @@ struct GridBarrier {
     int status;          // 0, or the code of a wait that gave up
 };
 
+// prepared grid arguments, one slot per grid (the larger, float64 form)
+static int64_t table_bytes(int32_t n_cfgs) {
+    return ((int64_t)n_cfgs * (int64_t)sizeof(GridEntry<double>) + 255) / 256 * 256;
+}
+
 static GridBarrier *barrier_of(const BatchLaunch &L) {
     return reinterpret_cast<GridBarrier *>(static_cast<char *>(L.workspace) + counters_bytes(L.n_cfgs));
 }
+template <typename T>
+static GridEntry<T> *table_of(const BatchLaunch &L) {
+    return reinterpret_cast<GridEntry<T> *>(static_cast<char *>(L.workspace) + counters_bytes(L.n_cfgs) +
+                                            kBarrierBytes);
+}
 static double *partials_of(const BatchLaunch &L) {
-    return reinterpret_cast<double *>(static_cast<char *>(L.workspace) + counters_bytes(L.n_cfgs) + kBarrierBytes);
+    return reinterpret_cast<double *>(static_cast<char *>(L.workspace) + counters_bytes(L.n_cfgs) + kBarrierBytes +
+                                      table_bytes(L.n_cfgs));
 }
 
 int batched_workspace_bytes(int32_t n_blocks, int32_t n_cfgs, int64_t *bytes) {
     if (n_blocks < 1 || n_cfgs < 1) return set_error(PIC_E_INVALID, "n_blocks and n_cfgs must be >= 1");
-    *bytes = counters_bytes(n_cfgs) + kBarrierBytes + (int64_t)n_blocks * 4 * 8;
+    *bytes = counters_bytes(n_cfgs) + kBarrierBytes + table_bytes(n_cfgs) + (int64_t)n_blocks * 4 * 8;
     return PIC_OK;
+}
+
+template <typename T>
+static int prep_table(const BatchLaunch &L, cudaStream_t st) {
+    batched_prep_kernel<T><<<(L.n_cfgs + 127) / 128, 128, 0, st>>>(L.cfgs, L.n_cfgs, table_of<T>(L));
+    return check_launch("batched_prep_kernel");
 }
 
 // Device-wide barrier of a cooperative launch (every block resident). The
@@ -251,7 +305,7 @@ struct BatchPersistArgs {
     const int64_t *step_task_off, *step_tracks;  // device, by global step
     const double *xs, *ys;
     uint32_t *counts;
-    int n_blocks;
+    int n_blocks, sms;
     int64_t first_step, n_steps;
     GridBarrier *bar;
 };
@@ -270,9 +324,11 @@ __global__ void __launch_bounds__(256) batched_persistent_kernel(BatchPersistArg
         const int bi = (int)(s & 1), bo = bi ^ 1;
         const int64_t t0 = p.step_task_off[s], t1 = p.step_task_off[s + 1], tracks = p.step_tracks[s];
         if (tracks > 0 && t1 > t0) {
-            for (int64_t w = (int64_t)blockIdx.x * WARPS + warp; w < tracks; w += (int64_t)gridDim.x * WARPS)
+            const int parts = deposit_parts(tracks, p.sms);
+            for (int64_t w = (int64_t)blockIdx.x * WARPS + warp; w < tracks * parts; w += (int64_t)gridDim.x * WARPS)
                 batched_deposit_warp<T>(p.b.cfgs, p.task_cfg + t0, p.task_first + t0, p.task_prefix + t0,
-                                        (int)(t1 - t0), w, p.xs, p.ys, (pair_t<T> *)p.dens[bi], p.counts, lane);
+                                        (int)(t1 - t0), w / parts, p.xs, p.ys, (pair_t<T> *)p.dens[bi], p.counts,
+                                        lane, (int)(w % parts), parts);
             if (!grid_barrier(p.bar)) return;
         }
         BatchStepArgs<T> b = p.b;
@@ -302,7 +358,10 @@ static int launch_persistent(const BatchLaunch &L, const int64_t *sto, const int
         }
     }
     BatchPersistArgs<T> p;
-    p.b = BatchStepArgs<T>{L.cfgs, L.blk_cfg, L.blk_item0, L.blk_item1, L.cfg_blk0, L.cfg_nblk, nullptr, nullptr,
+    int rc = prep_table<T>(L, st);
+    if (rc) return rc;
+    p.b = BatchStepArgs<T>{L.cfgs, table_of<T>(L), L.blk_cfg, L.blk_item0, L.blk_item1, L.cfg_blk0, L.cfg_nblk,
+                           nullptr, nullptr,
                            nullptr, nullptr, nullptr, nullptr, L.tally, partials_of(L),
                            reinterpret_cast<unsigned int *>(L.workspace), 0};
     for (int q = 0; q < 2; ++q) {
@@ -319,6 +378,7 @@ static int launch_persistent(const BatchLaunch &L, const int64_t *sto, const int
     p.ys = L.ys;
     p.counts = L.counts;
     p.n_blocks = L.n_blocks;
+    p.sms = sm_count();
     p.first_step = L.first_step;
     p.n_steps = L.n_steps;
     p.bar = barrier_of(L);
@@ -353,7 +413,7 @@ template <typename T, typename I>
 static void launch_batched_step(const BatchLaunch &L, int bi, int bo, double *partials, unsigned int *counters,
                                 int64_t step, cudaStream_t st) {
     constexpr int BLOCK = 256;
-    BatchStepArgs<T> b{L.cfgs, L.blk_cfg, L.blk_item0, L.blk_item1, L.cfg_blk0, L.cfg_nblk,
+    BatchStepArgs<T> b{L.cfgs, table_of<T>(L), L.blk_cfg, L.blk_item0, L.blk_item1, L.cfg_blk0, L.cfg_nblk,
                        (const T *)L.pos[bi], (const T *)L.neg[bi], (T *)L.pos[bo], (T *)L.neg[bo],
                        (const pair_t<T> *)L.dens[bi], (pair_t<T> *)L.dens[bo], L.tally, partials, counters, step};
     batched_step_kernel<T, BLOCK, I><<<(unsigned)L.n_blocks, BLOCK, 0, st>>>(b);
@@ -363,21 +423,27 @@ int batched_loop(const BatchLaunch &L, cudaStream_t st) {
     constexpr int WARPS = 8;
     unsigned int *counters = reinterpret_cast<unsigned int *>(L.workspace);
     double *partials = partials_of(L);
+    const int sms = sm_count();
+    if (L.n_steps > 0) {
+        int rc = L.dtype == PIC_F64 ? prep_table<double>(L, st) : prep_table<float>(L, st);
+        if (rc) return rc;
+    }
     for (int64_t s = 0; s < L.n_steps; ++s) {
         const int64_t step = L.first_step + s;
         const int bi = (int)(step & 1), bo = bi ^ 1;
         const int64_t t0 = L.step_task_off[s], t1 = L.step_task_off[s + 1];
         const int64_t tracks = L.step_tracks[s];
         if (tracks > 0 && t1 > t0) {
-            const unsigned blocks = (unsigned)((tracks + WARPS - 1) / WARPS);
+            const int parts = deposit_parts(tracks, sms);
+            const unsigned blocks = (unsigned)((tracks * parts + WARPS - 1) / WARPS);
             if (L.dtype == PIC_F64)
                 batched_deposit_kernel<double, WARPS><<<blocks, WARPS * 32, 0, st>>>(
                     L.cfgs, L.task_cfg + t0, L.task_first + t0, L.task_prefix + t0, (int)(t1 - t0), tracks, L.xs,
-                    L.ys, (double2 *)L.dens[bi], L.counts);
+                    L.ys, (double2 *)L.dens[bi], L.counts, parts);
             else
                 batched_deposit_kernel<float, WARPS><<<blocks, WARPS * 32, 0, st>>>(
                     L.cfgs, L.task_cfg + t0, L.task_first + t0, L.task_prefix + t0, (int)(t1 - t0), tracks, L.xs,
-                    L.ys, (float2 *)L.dens[bi], L.counts);
+                    L.ys, (float2 *)L.dens[bi], L.counts, parts);
             int rc = check_launch("batched_deposit_kernel");
             if (rc) return rc;
         }

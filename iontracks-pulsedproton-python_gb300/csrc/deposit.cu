@@ -42,14 +42,6 @@ __global__ void __launch_bounds__(WARPS * 32) deposit_kernel(const double *__res
     deposit_track<T>(xs[t], ys[t], n, dp, cut, h2b2, gfac, dens, counts, threadIdx.x & 31, warp % parts, parts);
 }
 
-// Warps per track: a step's tracks alone rarely fill the GPU (a few to a few
-// thousand per step), so with few tracks each box is shared by up to 8 warps.
-static int deposit_parts(int64_t m, int sms) {
-    const int64_t warps = (int64_t)sms * 32;  // half the resident warps of the GPU
-    int p = 8;
-    while (p > 1 && m * p > warps) p >>= 1;
-    return p;
-}
 
 int launch_deposit(const pic_grid *g, const double *xs, const double *ys, int64_t m, void *dens, uint32_t *counts,
                    cudaStream_t st) {

@@ -38,6 +38,16 @@ __host__ __device__ constexpr int stream_max_threads(int ipt) {
     return ipt <= 1 ? 17 * 32 : (ipt == 2 ? 13 * 32 : (ipt == 3 ? 11 * 32 : 9 * 32));
 }
 constexpr int kStreamMaxSmem = 227 * 1024;
+// Warps per track of a deposition: a step's tracks alone rarely fill the GPU
+// (a few to a few thousand per step), so with few tracks each box is shared by
+// up to 8 warps.
+__host__ __device__ inline int deposit_parts(int64_t m, int sms) {
+    const int64_t warps = (int64_t)sms * 32;  // half the resident warps of the GPU
+    int p = 8;
+    while (p > 1 && m * p > warps) p >>= 1;
+    return p;
+}
+
 // AUTO picks the streaming kernel from this many allocated cells (no_xy^2 * kpitch)
 constexpr int64_t kStreamMinCells = 200000000;
 
