@@ -62,6 +62,7 @@ struct AdjArgs {
     T p_lat, p_zm, p_zp, p_cen, n_lat, n_zm, n_zp, n_cen, a, gfac;
     T c_pos, c_neg;  // Courant numbers (zm - zp of each species)
     ScoreTest score;
+    FastDiv div_c4, div_n;  // item -> column -> (i, j) on the 32-bit path
 };
 
 template <typename I>
@@ -127,9 +128,16 @@ __global__ void __launch_bounds__(BLOCK) adjoint_step_kernel(AdjArgs<T> a) {
     const I n = (I)a.n, kp = (I)a.kp, c4 = (I)a.c4, dp = (I)a.dp, items = (I)a.items;
     const I stride = (I)gridDim.x * BLOCK;
     for (I item = (I)blockIdx.x * BLOCK + threadIdx.x; item < items; item += stride) {
-        const I col = item / c4;
+        I col, i;
+        if constexpr (sizeof(I) == 4) {
+            col = fast_div(item, a.div_c4);
+            i = fast_div(col, a.div_n);
+        } else {
+            col = item / c4;
+            i = col / n;
+        }
         const int c = (int)(item - col * c4);
-        const I i = col / n, j = col - i * n;
+        const I j = col - i * n;
         const int k0 = 4 * c;
         const I off = col * kp + k0;
         bool g[4], valid[4];
@@ -428,6 +436,8 @@ static int launch_adjoint_t(const pic_grid *g, const void *pos, const void *neg,
     a.gfac = (T)g->gaussian_factor;
     a.c_pos = (T)(g->p_zm - g->p_zp);
     a.c_neg = (T)(g->n_zm - g->n_zp);
+    a.div_c4 = make_fastdiv(a.c4);
+    a.div_n = make_fastdiv(a.n);
     int rc = score_test(g, &a.score);
     if (rc) return rc;
     const int64_t blocks = adjoint_blocks(g);

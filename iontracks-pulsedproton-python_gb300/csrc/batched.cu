@@ -78,6 +78,8 @@ __device__ void grid_args(const pic_batch_cfg &C, StepArgs<T> &a) {
     const double r4 = 4.0 * g.scoring_radius_sq;
     a.score.thr4 = r4 >= 4.0e18 ? (int64_t)4.0e18 : (int64_t)ceil(r4) - 1;
     a.injected_scale = (double)g.no_z;
+    a.div_c4 = make_fastdiv(a.c4);
+    a.div_n = make_fastdiv(a.n);
 }
 
 template <typename T>

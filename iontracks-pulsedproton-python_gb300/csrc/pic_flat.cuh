@@ -26,6 +26,7 @@ struct StepArgs {
     T p_lat, p_zm, p_zp, p_cen, n_lat, n_zm, n_zp, n_cen, alpha_dt, gfac;
     ScoreTest score;
     double injected_scale;  // no_z: the pairs carry G already
+    FastDiv div_c4, div_n;  // item -> column -> (i, j) on the 32-bit path
 };
 
 template <typename T>
@@ -62,9 +63,16 @@ __device__ __forceinline__ void flat_item(const StepArgs<T> &a, I item, Tally<T>
                                           Tally<T> &t_p, Tally<T> &t_n, Tally<T> &t_inj) {
     auto ld4 = [](const T *p) { return COH ? load4c(p) : load4(p); };
     const I n = (I)a.n, kp = (I)a.kp, c4 = (I)a.c4, dp = (I)a.dp;
-    const I col = item / c4;
+    I col, i;
+    if constexpr (sizeof(I) == 4) {
+        col = fast_div(item, a.div_c4);
+        i = fast_div(col, a.div_n);
+    } else {
+        col = item / c4;
+        i = col / n;
+    }
     const int c = (int)(item - col * c4);
-    const I i = col / n, j = col - i * n;
+    const I j = col - i * n;
     const int k0 = 4 * c;
     if (c == 0 && a.dens_zero) a.dens_zero[i * dp + j] = pair_t<T>{T(0), T(0)};
 

@@ -38,6 +38,25 @@ __host__ __device__ constexpr int stream_max_threads(int ipt) {
     return ipt <= 1 ? 17 * 32 : (ipt == 2 ? 13 * 32 : (ipt == 3 ? 11 * 32 : 9 * 32));
 }
 constexpr int kStreamMaxSmem = 227 * 1024;
+// Division by an invariant divisor d >= 1 of dividends n < 2^31, by one
+// multiply and shift (T. Granlund and P. Montgomery, "Division by invariant
+// integers using multiplication", PLDI 1994): with l = ceil(log2 d) and
+// m = ceil(2^(31+l) / d), n / d = (n * m) >> (31 + l) exactly (m < 2^33, so
+// the product fits 64 bits).
+struct FastDiv {
+    uint64_t m;
+    int sh;
+};
+__host__ __device__ inline FastDiv make_fastdiv(int64_t d) {
+    int l = 0;
+    while (((int64_t)1 << l) < d) ++l;
+    const int sh = 31 + l;
+    return FastDiv{(((uint64_t)1 << sh) + (uint64_t)d - 1) / (uint64_t)d, sh};
+}
+__host__ __device__ __forceinline__ uint32_t fast_div(uint32_t n, FastDiv f) {
+    return (uint32_t)(((unsigned long long)n * f.m) >> f.sh);
+}
+
 // Warps per track of a deposition: a step's tracks alone rarely fill the GPU
 // (a few to a few thousand per step), so with few tracks each box is shared by
 // up to 8 warps.

@@ -78,6 +78,8 @@ static int launch_step_t(const pic_grid *g, const void *pos_in, const void *neg_
     int rc = score_test(g, &a.score);
     if (rc) return rc;
     a.injected_scale = (double)g->no_z;
+    a.div_c4 = make_fastdiv(a.c4);
+    a.div_n = make_fastdiv(a.n);
     int64_t blocks = (a.items + BLOCK - 1) / BLOCK;
     const int64_t cap = step_grid_cap(g->dtype == PIC_F64 ? 1 : 0);
     if (blocks > cap) blocks = cap;
