@@ -216,11 +216,14 @@ def run_sweep(args):
     batch = pkg.run_batched_b200(cfgs)
     torch.cuda.synchronize()
     t_batch = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    plain = [pkg.run_simulation_b200(c, progress=False, return_fields=False) for c in cfgs]
-    torch.cuda.synchronize()
-    t_plain = time.perf_counter() - t0
-    dks = max(abs(b.ks - p.ks) for b, p in zip(batch, plain))
+    if args.batched_only:
+        plain, t_plain, dks = None, None, None
+    else:
+        t0 = time.perf_counter()
+        plain = [pkg.run_simulation_b200(c, progress=False, return_fields=False) for c in cfgs]
+        torch.cuda.synchronize()
+        t_plain = time.perf_counter() - t0
+        dks = max(abs(b.ks - p.ks) for b, p in zip(batch, plain))
     if rank == 0:
         line = {
             "metric": "interior voxel-steps/s, 64-config saturation sweep", "value": vox / t_batch,
@@ -230,7 +233,8 @@ def run_sweep(args):
             "config": {"workload": f"saturation sweep: {len(cfgs)} of 64 configs, 25-400 V log-spaced, gaps "
                                    "0.1/0.2/0.3 cm, 1-100 Gy/s, 100-1000 us pulses, 5/10 um voxels, "
                                    "r 0.008-0.03 cm, seeds 1-64", "interior_voxel_steps": vox},
-            "batched_s": t_batch, "sequential_plain_s": t_plain, "speedup_vs_sequential": t_plain / t_batch,
+            "batched_s": t_batch, "sequential_plain_s": t_plain,
+            "speedup_vs_sequential": None if t_plain is None else t_plain / t_batch,
             "max_abs_dks_batched_vs_plain": dks,
         }
         print(json.dumps(line), flush=True)
@@ -438,6 +442,8 @@ def main():
     ap.add_argument("--ref-max-steps", dest="ref_max_steps", type=int, default=300,
                     help="--impl reference: at most this many timed steps")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--batched-only", dest="batched_only", action="store_true",
+                    help="saturation_sweep: time the batched run only (profiling)")
     ap.add_argument("--sweep-configs", dest="sweep_configs", type=int, default=64,
                     help="saturation_sweep: run the first N of the 64 configurations (profiling-size cases)")
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner")

@@ -138,9 +138,16 @@ __device__ __forceinline__ void batched_step_block(const BatchStepArgs<T> &b, in
     }
     __syncthreads();
     Tally<T> t_rec, t_p, t_n, t_inj;
-    const I i1 = (I)b.blk_item1[blk];
-    for (I item = (I)b.blk_item0[blk] + threadIdx.x; item < i1; item += BLOCK)
-        flat_item<T, I, COH>(a, item, t_rec, t_p, t_n, t_inj);
+    // The grid's blocks stride through its items together (block r of nb
+    // takes items r*BLOCK + t + k*nb*BLOCK): resident blocks of a grid then
+    // sweep one contiguous front through it, and each item's i-1 / i+1
+    // neighbours are read while still in L2 (a contiguous chunk per block left
+    // hundreds of separate windows in flight across the batch).
+    {
+        const I r = (I)(blk - b.cfg_blk0[c]), stride = (I)b.cfg_nblk[c] * BLOCK, items = (I)a.items;
+        for (I item = r * BLOCK + threadIdx.x; item < items; item += stride)
+            flat_item<T, I, COH>(a, item, t_rec, t_p, t_n, t_inj);
+    }
     R v[4] = {red_of(t_inj), red_of(t_rec), red_of(t_p), red_of(t_n)};
     block_sum4<BLOCK>(v, red);
     if (threadIdx.x == 0) {
