@@ -34,6 +34,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -97,7 +98,8 @@ class ClockSampler:
     def __init__(self, gpu_index=0):
         self.proc = None
         self.gpu = gpu_index
-        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+        # raw samples (the JSON line carries their summary); PIC_CLOCKS_DIR keeps them
+        self.path = Path(os.environ.get("PIC_CLOCKS_DIR", tempfile.gettempdir())) / f"pic_clocks_{os.getpid()}.csv"
 
     def __enter__(self):
         try:
