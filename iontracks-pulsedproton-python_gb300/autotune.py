@@ -38,7 +38,7 @@ def candidate_shapes(grid, quick: bool = False) -> list[dict]:
     tjs = (3, 5, 7, 10) if quick else (2, 3, 4, 5, 6, 7, 8, 10, 12)
     cws = (8, 12, 16) if quick else (4, 6, 8, 10, 12, 16)
     planes = (4, 16, 64) if quick else (4, 8, 16, 32, 64, 128)
-    stage_counts = (4, 6, 8) if quick else (4, 5, 6, 8, 10, 12, 16)
+    stage_counts = (4, 5, 6, 8) if quick else (4, 5, 6, 8, 10, 12, 16)
     for tj, cw, ctas, stages, li in itertools.product(tjs, cws, (1, 2), stage_counts, planes):
         if tj > grid.no_xy - 2:
             continue
