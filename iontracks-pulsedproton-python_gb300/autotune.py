@@ -35,7 +35,7 @@ def candidate_shapes(grid, quick: bool = False) -> list[dict]:
         return out
     out.append({"variant": "stream"})  # the library's own default shape
     kp = grid.kpitch
-    tjs = (3, 5, 7, 10) if quick else (2, 3, 4, 5, 6, 7, 8, 10, 12)
+    tjs = (3, 5, 7, 10, 12) if quick else (2, 3, 4, 5, 6, 7, 8, 10, 12, 14)
     cws = (8, 12, 16) if quick else (4, 6, 8, 10, 12, 16)
     planes = (4, 16, 64) if quick else (4, 8, 16, 32, 64, 128)
     stage_counts = (4, 5, 6, 8) if quick else (4, 5, 6, 8, 10, 12, 16)
@@ -46,9 +46,9 @@ def candidate_shapes(grid, quick: bool = False) -> list[dict]:
         if ctas * (smem + 3 * 1024) > _SMEM_PER_SM:
             continue
         ipt = -(-(tj * (kp // 4)) // (cw * 32))
-        if ipt > 4 or (cw + 1) * 32 > (544, 416, 352, 288)[ipt - 1]:
+        if ipt > 6 or (cw + 1) * 32 > (544, 416, 352, 288, 288, 288)[ipt - 1]:
             continue
-        regs = (96, 128, 144, 160)[ipt - 1]
+        regs = (96, 128, 152, 168, 168, 168)[ipt - 1]
         if ctas * (cw + 1) * 32 * regs > 65536:
             continue
         out.append(dict(variant="stream", tile_rows=tj, consumer_warps=cw, ctas_per_sm=ctas, stages=stages,

@@ -103,8 +103,9 @@ int resolve_shape(pic_grid *g) {
         g->tile_rows = tj;
     }
     if (g->tile_rows > (int)g->no_xy - 2) g->tile_rows = (int)g->no_xy - 2;
-    if (g->tile_rows * c4 > 4 * nct)
-        return set_error(PIC_E_INVALID, "stream variant: tile_rows * kpitch/4 must be <= 4 * 32 * consumer_warps");
+    if (g->tile_rows * c4 > kStreamMaxIpt * nct)
+        return set_error(PIC_E_INVALID, "stream variant: tile_rows * kpitch/4 must be <= " +
+                                            std::to_string(kStreamMaxIpt) + " * 32 * consumer_warps");
     {
         const int ipt = (g->tile_rows * c4 + nct - 1) / nct;
         if (nct + 32 > stream_max_threads(ipt))

@@ -37,6 +37,8 @@ constexpr int kStreamMaxThreads = 17 * 32;
 __host__ __device__ constexpr int stream_max_threads(int ipt) {
     return ipt <= 1 ? 17 * 32 : (ipt == 2 ? 13 * 32 : (ipt == 3 ? 11 * 32 : 9 * 32));
 }
+// items (k-vectors of a plane) per consumer thread: 1 .. kStreamMaxIpt
+constexpr int kStreamMaxIpt = 6;
 constexpr int kStreamMaxSmem = 227 * 1024;
 // Division by an invariant divisor d >= 1 of dividends n < 2^31, by one
 // multiply and shift (T. Granlund and P. Montgomery, "Division by invariant

@@ -525,15 +525,17 @@ int launch_stream_step(const pic_grid *g, const StreamShape &sh, const void *pos
     if (blocks > kMaxStepBlocks) blocks = kMaxStepBlocks;
     const int threads = (a.consumer_warps + 1) * 32;
     const int ipt = (a.tj * a.c4 + a.consumer_warps * 32 - 1) / (a.consumer_warps * 32);
-    if (ipt >= 1 && ipt <= 4 && threads > stream_max_threads(ipt))
+    if (ipt >= 1 && ipt <= kStreamMaxIpt && threads > stream_max_threads(ipt))
         return set_error(PIC_E_INVALID, "stream variant: too many consumer warps for this tile (registers)");
     switch (ipt) {
         case 1: return launch_ipt<1>(a, (unsigned)blocks, threads, smem, st);
         case 2: return launch_ipt<2>(a, (unsigned)blocks, threads, smem, st);
         case 3: return launch_ipt<3>(a, (unsigned)blocks, threads, smem, st);
         case 4: return launch_ipt<4>(a, (unsigned)blocks, threads, smem, st);
+        case 5: return launch_ipt<5>(a, (unsigned)blocks, threads, smem, st);
+        case 6: return launch_ipt<6>(a, (unsigned)blocks, threads, smem, st);
         default:
-            return set_error(PIC_E_INVALID, "stream variant: tile_rows x k-vectors exceed 4 items per consumer thread");
+            return set_error(PIC_E_INVALID, "stream variant: tile_rows x k-vectors exceed 6 items per consumer thread");
     }
 }
 
