@@ -299,7 +299,8 @@ def run_gb300(args):
     eng_mod = importlib.import_module(PACKAGE + ".engine")
     native = importlib.import_module(PACKAGE + "._native")
     desc, cfg = _config(args.workload)
-    rng = np.random.default_rng(cfg.seed + rank)
+    replicas = importlib.import_module(PACKAGE + ".replicas")
+    rng = np.random.default_rng(replicas.replica_seed(cfg.seed, rank))
     sched = pkg.build_track_schedule(cfg, rng)
     n_steps = args.warmup + args.steps
     if n_steps > cfg.pulse_time_steps:
@@ -333,13 +334,12 @@ def run_gb300(args):
         t_end.record(stream)
         torch.cuda.synchronize()
     ms = t_start.elapsed_time(t_end)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        dist.barrier()
     vox = _interior(cfg)
-    value = vox * args.steps * world / (ms / 1e3)
+    # all ranks' voxel-steps over the slowest rank's time
+    value = replicas.whole_job_rate(vox * args.steps, ms / 1e3)
+    ms = replicas.max_over_ranks(ms)
+    if world > 1:
+        dist.barrier()
     launches = 2 * int((counts[args.warmup:] > 0).sum()) + int((counts[args.warmup:] == 0).sum())
 
     # dominant kernel: the fused step, one launch per step, event-timed on
@@ -378,12 +378,14 @@ def run_gb300(args):
     if rank == 0 or world > 1:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        res = pkg.run_simulation_b200(cfg, rng=np.random.default_rng(cfg.seed + rank), progress=False,
-                                      max_steps=args.e2e_steps, return_fields=False, shape=shape)
+        res = pkg.run_simulation_b200(cfg, rng=np.random.default_rng(replicas.replica_seed(cfg.seed, rank)),
+                                      progress=False, max_steps=args.e2e_steps, return_fields=False, shape=shape)
         torch.cuda.synchronize()
         e2e_s = time.perf_counter() - t0
         tracks = float(sched[: args.e2e_steps].sum())
-        e2e = {"value": vox * res.steps_completed * world / e2e_s, "unit": "voxel-steps/s",
+        e2e_rate = replicas.whole_job_rate(vox * res.steps_completed, e2e_s)
+        e2e_s = replicas.max_over_ranks(e2e_s)
+        e2e = {"value": e2e_rate, "unit": "voxel-steps/s",
                "h2d_bytes_per_step": 16.0 * tracks / args.e2e_steps, "d2h_bytes_per_step": 32,
                "steps": int(res.steps_completed), "wall_s": e2e_s,
                "includes": "schedule + track sampling on the host, H2D of tracks, all steps, D2H of tallies"}
