@@ -300,6 +300,69 @@ def run_adjoint(args):
     return 0
 
 
+def run_adjoint_full(args):
+    """Forward + adjoint of the 5 um full electrode (1068 x 1068 x 406) under
+    a device-memory limit (default 180 GB): the binomial schedule with as many
+    float32 state slots as fit, over the first --adjoint-steps steps (the
+    whole 985 801-step run takes hours: its cost is projected from the
+    measured per-step times and the schedule's exact recomputation count).
+    One plain forward solve of the same steps is timed beside it."""
+    import torch
+
+    world, rank = _dist()
+    pkg = _pkg()
+    adj = importlib.import_module(PACKAGE + ".adjoint")
+    desc, cfg = _config(args.adjoint_workload)
+    n = int(args.adjoint_steps)
+    limit = float(args.memory_limit_gb) * 1e9
+    for _ in range(max(1, args.warmup)):
+        adj.ks_and_gradient(cfg, max_steps=min(n, 8), memory_limit=limit)
+        torch.cuda.empty_cache()
+    runs, plain = [], []
+    for _ in range(max(1, args.steps)):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        res = pkg.run_simulation_b200(cfg, progress=False, return_fields=False, max_steps=n)
+        torch.cuda.synchronize()
+        plain.append(time.perf_counter() - t)
+        del res
+        torch.cuda.empty_cache()
+        torch.cuda.reset_peak_memory_stats()
+        base = torch.cuda.memory_allocated()
+        t = time.perf_counter()
+        ks, grad, tm = adj.ks_and_gradient(cfg, max_steps=n, memory_limit=limit)
+        torch.cuda.synchronize()
+        tm["total_s"] = time.perf_counter() - t
+        tm["peak_bytes"] = torch.cuda.max_memory_allocated() - base
+        runs.append((ks, grad, tm))
+        torch.cuda.empty_cache()
+    med = lambda key: statistics.median(r[2][key] for r in runs)  # noqa: E731
+    plan = runs[-1][2]["plan"]
+    t_step = med("forward_device_s") / n
+    t_adj = (med("backward_device_s") - plan["recompute_steps"] * t_step) / n
+    full = int(cfg.total_time_steps)
+    rec_full, _ = adj.revolve_plan(full, plan["slots"])
+    proj = full * t_step + rec_full * t_step + full * t_adj
+    if rank == 0:
+        ks, grad, _ = runs[-1]
+        print(json.dumps({
+            "metric": "forward + adjoint wall time / one plain forward solve (same steps)",
+            "value": statistics.median(r[2]["total_s"] for r in runs) / statistics.median(plain), "unit": "x",
+            "n_gpus": world, "steps": len(runs), "warmup": args.warmup, "ms_per_step": None,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": desc + f"; first {n} steps; device memory limit {limit / 1e9:.0f} GB",
+                       "parameters": list(adj.PARAMS)},
+            "plan": plan, "peak_device_bytes": max(r[2]["peak_bytes"] for r in runs),
+            "plain_forward_s": statistics.median(plain), "adjoint_total_s": med("total_s"),
+            "forward_device_s": med("forward_device_s"), "backward_device_s": med("backward_device_s"),
+            "step_ms": 1e3 * t_step, "adjoint_step_ms": 1e3 * t_adj,
+            "full_run": {"steps": full, "slots": plan["slots"], "recompute_steps": rec_full,
+                         "projected_s": proj, "projected_vs_forward": proj / (full * t_step)},
+            "ks": ks, "dks_dtheta": list(grad),
+        }), flush=True)
+    return 0
+
+
 def run_gb300(args):
     import torch
     import torch.distributed as dist
@@ -452,7 +515,7 @@ def main():
     ap.add_argument("--steps", type=int, default=600)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["saturation_sweep", "adjoint"], default="full_electrode_5um")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["saturation_sweep", "adjoint", "adjoint_full_electrode"], default="full_electrode_5um")
     ap.add_argument("--dtype", choices=["float32", "float64"], default="float32")
     ap.add_argument("--e2e-steps", type=int, default=600)
     ap.add_argument("--cpu-steps", dest="cpu_steps", type=int, default=50,
@@ -464,6 +527,12 @@ def main():
                     help="saturation_sweep: time the batched run only (profiling)")
     ap.add_argument("--sweep-configs", dest="sweep_configs", type=int, default=64,
                     help="saturation_sweep: run the first N of the 64 configurations (profiling-size cases)")
+    ap.add_argument("--adjoint-steps", dest="adjoint_steps", type=int, default=1000,
+                    help="adjoint_full_electrode: steps of the run differentiated")
+    ap.add_argument("--adjoint-workload", dest="adjoint_workload", choices=sorted(WORKLOADS),
+                    default="full_electrode_5um", help="adjoint_full_electrode: the chamber (profiling-size cases)")
+    ap.add_argument("--memory-limit-gb", dest="memory_limit_gb", type=float, default=180.0,
+                    help="adjoint_full_electrode: device memory the gradient may hold")
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner")
     ap.add_argument("--variant", choices=["auto", "flat", "stream"], default="auto")
     ap.add_argument("--tile-rows", dest="tile_rows", type=int, default=0)
@@ -480,6 +549,8 @@ def main():
         return run_sweep(args)
     if args.workload == "adjoint":
         return run_adjoint(args)
+    if args.workload == "adjoint_full_electrode":
+        return run_adjoint_full(args)
     return run_gb300(args)
 
 

@@ -275,6 +275,50 @@ int pic_adjoint_backward(const pic_grid *g, const void *ckpt_pos, const void *ck
                          int64_t workspace_bytes, void *adj_workspace, int64_t adj_workspace_bytes, uintptr_t stream);
 
 /*
+ * Binomial checkpointing (no counterpart in the reference, which has no
+ * adjoint): the gradient of a run too long for pic_adjoint_forward/_backward's
+ * kept densities and checkpoint segments, in a fixed number of state slots.
+ * The schedule is the binomial one of Griewank ("revolve", ACM TOMS 26, 2000):
+ * with n_slots slots (the initial state's included), n_steps steps are
+ * reversed with the fewest recomputed steps; no deposition is kept, a
+ * recomputed step deposits its tracks again into the one scratch pair buffer
+ * `dens` ([no_xy][pic_dens_pitch] pairs, 16-byte aligned).
+ *
+ * pic_revolve_plan -- no device work: *recompute_steps = the steps the
+ * backward pass recomputes, *spine_levels = the states the forward stores.
+ * pic_revolve_spine -- the steps whose states the forward stores, slot q
+ * holding steps[q] (up to cap entries; *n_levels = how many).
+ * pic_revolve_trace -- no device work: runs the backward schedule against a
+ * bookkeeping of the slots, failing if any step's adjoint would run without
+ * its state; events[4*e ..] = (1, s0, n, slot or -1) for "advance n steps
+ * from step s0" and (2, s, slot or -1, 0) for "adjoint step s" (up to cap
+ * events; *n_events = how many); *advanced = recomputed steps.
+ *
+ * pic_revolve_forward -- the forward pass: as pic_adjoint_forward (state s in
+ * pair s & 1, tallies into tally[4*s ..], histogram into counts), storing the
+ * spine states into slots_pos/neg + slot * state_stride elements.
+ * pic_revolve_backward -- the reverse sweep from those slots (same n_steps,
+ * n_slots, tracks): work_* are two scratch field pairs (e.g. the forward's),
+ * lambda as pic_adjoint_backward (zeroed by the caller, starts in buffer 0,
+ * lambda_0 ends in buffer n_steps & 1), grad[0..4] = dR/d(s+, c+, s-, c-,
+ * alpha_dt) summed over all steps.
+ */
+int pic_revolve_plan(int64_t n_steps, int64_t n_slots, int64_t *recompute_steps, int64_t *spine_levels);
+int pic_revolve_spine(int64_t n_steps, int64_t n_slots, int64_t *steps, int64_t cap, int64_t *n_levels);
+int pic_revolve_trace(int64_t n_steps, int64_t n_slots, int64_t *events, int64_t cap, int64_t *n_events,
+                      int64_t *advanced);
+int pic_revolve_forward(const pic_grid *g, void *pos0, void *neg0, void *pos1, void *neg1, int64_t n_steps,
+                        const double *xs, const double *ys, const int64_t *track_offsets, void *dens,
+                        uint32_t *counts, double *tally, void *slots_pos, void *slots_neg, int64_t state_stride,
+                        int64_t n_slots, void *workspace, int64_t workspace_bytes, uintptr_t stream);
+int pic_revolve_backward(const pic_grid *g, void *slots_pos, void *slots_neg, int64_t state_stride, int64_t n_slots,
+                         int64_t n_steps, const double *xs, const double *ys, const int64_t *track_offsets,
+                         void *dens, void *work_pos0, void *work_neg0, void *work_pos1, void *work_neg1,
+                         void *lam_pos0, void *lam_neg0, void *lam_pos1, void *lam_neg1, double *grad,
+                         void *workspace, int64_t workspace_bytes, void *adj_workspace, int64_t adj_workspace_bytes,
+                         uintptr_t stream);
+
+/*
  * pic_capture_begin / pic_capture_end -- record every launch the library
  * issues on `stream` between the two calls (made from this host thread) into
  * a CUDA graph, instantiated and returned in *graph_out (replay with

@@ -39,13 +39,12 @@
 
 #include <string>
 
+#include "pic_adjoint.cuh"
 #include "pic_device.cuh"
 #include "pic_flat.cuh"
 #include "pic_internal.h"
 
 namespace pic {
-
-constexpr int kAdjGrad = 5;  // dR/ds+, dR/dc+, dR/ds-, dR/dc-, dR/da
 
 template <typename T>
 struct AdjArgs {
@@ -68,31 +67,6 @@ struct AdjArgs {
 template <typename I>
 __device__ __forceinline__ bool interior_col(I i, I j, I n) {
     return i >= 1 && j >= 1 && i <= n - 2 && j <= n - 2;
-}
-
-// Reduction helpers over kAdjGrad values (double-float for float32 fields).
-template <typename T> struct AdjRed { using type = double; };
-template <> struct AdjRed<float> { using type = DF; };
-__device__ __forceinline__ double adj_of(const Tally<double> &t) { return t.value(); }
-__device__ __forceinline__ DF adj_of(const Tally<float> &t) { return df_of(t); }
-__device__ __forceinline__ void adj_store(double *slot, double v) { *slot = v; }
-__device__ __forceinline__ void adj_store(double *slot, DF v) {
-    *reinterpret_cast<float2 *>(slot) = make_float2(v.hi, v.lo);
-}
-__device__ __forceinline__ void adj_load_add(double &acc, const double *slot) { acc += __ldcg(slot); }
-__device__ __forceinline__ void adj_load_add(DF &acc, const double *slot) {
-    const float2 p = __ldcg(reinterpret_cast<const float2 *>(slot));
-    acc = df_add(acc, DF{p.x, p.y});
-}
-__device__ __forceinline__ double adj_value(double v) { return v; }
-__device__ __forceinline__ double adj_value(DF v) { return df_value(v); }
-// slot += v, by the one thread that owns the slot
-__device__ __forceinline__ void adj_accumulate(double *slot, double v) { *slot += v; }
-__device__ __forceinline__ void adj_accumulate(double *slot, DF v) {
-    float2 *p = reinterpret_cast<float2 *>(slot);
-    const float2 o = *p;
-    const DF s = df_add(DF{o.x, o.y}, v);
-    *p = make_float2(s.hi, s.lo);
 }
 
 template <int BLOCK, typename A>
@@ -378,7 +352,9 @@ __global__ void adjoint_fold_kernel(T *lp, T *ln, int64_t n, int64_t kp, int64_t
     store4(ln + (ci * n + cj) * kp + k0, sn);
 }
 
+// The adjoint workspace: [counter at 0 | status at 64 | .. 256 | slots].
 static int64_t adj_counter_bytes() { return 256; }
+static int64_t adj_status_offset() { return 64; }
 
 int adjoint_workspace_bytes(int64_t *bytes) {
     *bytes = adj_counter_bytes() + (int64_t)kMaxStepBlocks * kAdjGrad * 8;
@@ -408,6 +384,13 @@ static int launch_adjoint_t(const pic_grid *g, const void *pos, const void *neg,
                                                                                  n_edge);
         int rc = check_launch("adjoint_fold_kernel");
         if (rc) return rc;
+    }
+    if (sizeof(T) == 4 && adjoint_stream_eligible(g)) {
+        char *w = static_cast<char *>(ws);
+        return launch_adjoint_stream(g, pos, neg, dens, lp_in, ln_in, lp_out, ln_out, grad,
+                                     reinterpret_cast<unsigned int *>(w), reinterpret_cast<int *>(w + adj_status_offset()),
+                                     reinterpret_cast<double *>(w + adj_counter_bytes()), adjoint_blocks(g), st,
+                                     accumulate);
     }
     AdjArgs<T> a;
     a.pos = (const T *)pos;

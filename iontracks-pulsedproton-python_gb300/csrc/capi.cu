@@ -508,6 +508,77 @@ int pic_adjoint_backward(const pic_grid *g, const void *ckpt_pos, const void *ck
     return adjoint_accumulate_end(g, adj_workspace, grad, st);
 }
 
+int pic_revolve_plan(int64_t n_steps, int64_t n_slots, int64_t *recompute_steps, int64_t *spine_levels) {
+    return revolve_plan(n_steps, n_slots, recompute_steps, spine_levels);
+}
+
+int pic_revolve_spine(int64_t n_steps, int64_t n_slots, int64_t *steps, int64_t cap, int64_t *n_levels) {
+    if (!n_levels || (cap > 0 && !steps)) return set_error(PIC_E_INVALID, "null pointer argument");
+    return revolve_spine(n_steps, n_slots, steps, cap, n_levels);
+}
+
+int pic_revolve_trace(int64_t n_steps, int64_t n_slots, int64_t *events, int64_t cap, int64_t *n_events,
+                      int64_t *advanced) {
+    if (!n_events || !advanced || (cap > 0 && !events)) return set_error(PIC_E_INVALID, "null pointer argument");
+    return revolve_trace(n_steps, n_slots, events, cap, n_events, advanced);
+}
+
+// Checks shared by the two revolve passes: slots, stride, offsets, scratch.
+static int check_revolve(const pic_grid *g, const void *slots_pos, const void *slots_neg, int64_t state_stride,
+                         int64_t n_slots, int64_t n_steps, const double *xs, const double *ys,
+                         const int64_t *track_offsets, const void *dens) {
+    int rc = check_grid(g);
+    if (rc) return rc;
+    if ((rc = check_fields(slots_pos, slots_neg, slots_pos, slots_neg))) return rc;
+    if (n_steps < 0 || n_slots < 1) return set_error(PIC_E_INVALID, "n_steps must be >= 0 and n_slots >= 1");
+    if (!track_offsets) return set_error(PIC_E_INVALID, "track_offsets is null");
+    const int64_t field = g->no_xy * g->no_xy * g->kpitch;
+    if (state_stride < field || state_stride % 8 != 0)
+        return set_error(PIC_E_INVALID, "state_stride must be >= no_xy^2 * kpitch and a multiple of 8 elements");
+    int64_t n_dep = 0;
+    if ((rc = kept_slots(track_offsets, n_steps, &n_dep))) return rc;
+    if (n_dep > 0 && (!xs || !ys || !dens)) return set_error(PIC_E_INVALID, "track or deposition arrays are null");
+    if (n_dep > 0 && !aligned(dens, 16)) return set_error(PIC_E_INVALID, "the deposition scratch must be 16-byte aligned");
+    return revolve_plan(n_steps, n_slots, nullptr, nullptr);
+}
+
+int pic_revolve_forward(const pic_grid *g, void *pos0, void *neg0, void *pos1, void *neg1, int64_t n_steps,
+                        const double *xs, const double *ys, const int64_t *track_offsets, void *dens,
+                        uint32_t *counts, double *tally, void *slots_pos, void *slots_neg, int64_t state_stride,
+                        int64_t n_slots, void *workspace, int64_t workspace_bytes, uintptr_t stream) {
+    int rc = check_revolve(g, slots_pos, slots_neg, state_stride, n_slots, n_steps, xs, ys, track_offsets, dens);
+    if (rc) return rc;
+    if ((rc = check_fields(pos0, neg0, pos1, neg1))) return rc;
+    if (!counts || !tally) return set_error(PIC_E_INVALID, "null pointer argument");
+    if (!workspace || workspace_bytes < kWorkspaceBytes)
+        return set_error(PIC_E_INVALID, "workspace too small (pic_step_workspace_bytes)");
+    return revolve_forward(g, pos0, neg0, pos1, neg1, n_steps, xs, ys, track_offsets, dens, counts, tally, slots_pos,
+                           slots_neg, state_stride, n_slots, workspace, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int pic_revolve_backward(const pic_grid *g, void *slots_pos, void *slots_neg, int64_t state_stride, int64_t n_slots,
+                         int64_t n_steps, const double *xs, const double *ys, const int64_t *track_offsets,
+                         void *dens, void *work_pos0, void *work_neg0, void *work_pos1, void *work_neg1,
+                         void *lam_pos0, void *lam_neg0, void *lam_pos1, void *lam_neg1, double *grad,
+                         void *workspace, int64_t workspace_bytes, void *adj_workspace, int64_t adj_workspace_bytes,
+                         uintptr_t stream) {
+    int rc = check_revolve(g, slots_pos, slots_neg, state_stride, n_slots, n_steps, xs, ys, track_offsets, dens);
+    if (rc) return rc;
+    if ((rc = check_fields(work_pos0, work_neg0, work_pos1, work_neg1)) ||
+        (rc = check_fields(lam_pos0, lam_neg0, lam_pos1, lam_neg1)))
+        return rc;
+    if (!grad) return set_error(PIC_E_INVALID, "grad is null");
+    if (!workspace || workspace_bytes < kWorkspaceBytes)
+        return set_error(PIC_E_INVALID, "workspace too small (pic_step_workspace_bytes)");
+    int64_t need = 0;
+    adjoint_workspace_bytes(&need);
+    if (!adj_workspace || adj_workspace_bytes < need)
+        return set_error(PIC_E_INVALID, "adjoint workspace too small (pic_adjoint_workspace_bytes)");
+    return revolve_backward(g, slots_pos, slots_neg, state_stride, n_slots, n_steps, xs, ys, track_offsets, dens,
+                            work_pos0, work_neg0, work_pos1, work_neg1, lam_pos0, lam_neg0, lam_pos1, lam_neg1, grad,
+                            workspace, adj_workspace, reinterpret_cast<cudaStream_t>(stream));
+}
+
 int pic_run_segment(const pic_grid *g, void *pos0, void *neg0, void *pos1, void *neg1, int64_t parity,
                     int64_t n_steps, const double *xs, const double *ys, const int64_t *track_offsets,
                     void *dens0, void *dens1, int64_t dens_parity, uint32_t *counts, double *tally,

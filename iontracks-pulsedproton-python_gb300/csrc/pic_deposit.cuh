@@ -43,8 +43,9 @@ __device__ __forceinline__ void deposit_track(double x, double y, int64_t n, int
     j_lo = j_lo < 0 ? 0 : j_lo;
     i_hi = i_hi > n ? n : i_hi;
     j_hi = j_hi > n ? n : j_hi;
-    if (lane == 0 && part == 0) {
-        // int(x) floors for x >= 0; centres lie in [0, no_xy).
+    if (counts && lane == 0 && part == 0) {
+        // int(x) floors for x >= 0; centres lie in [0, no_xy). A recomputed
+        // step passes no counter: its tracks were counted once.
         int64_t ix = (int64_t)x, iy = (int64_t)y;
         if (ix >= 0 && ix < n && iy >= 0 && iy < n) atomicAdd(counts + ix * n + iy, 1u);
     }

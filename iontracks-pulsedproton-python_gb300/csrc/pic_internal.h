@@ -134,7 +134,28 @@ int adjoint_workspace_bytes(int64_t *bytes);
 int launch_adjoint(const pic_grid *g, const void *pos, const void *neg, const void *dens, void *lp_in, void *ln_in,
                    void *lp_out, void *ln_out, double *grad, void *ws, cudaStream_t st, bool accumulate = false);
 int adjoint_accumulate_begin(const pic_grid *g, void *ws, cudaStream_t st);
+// The streaming adjoint (adjoint_stream.cu): float32 grids that run the
+// streaming forward step (variant STREAM, or AUTO at kStreamMinCells cells).
+bool adjoint_stream_eligible(const pic_grid *g);
+int launch_adjoint_stream(const pic_grid *g, const void *pos, const void *neg, const void *dens, const void *lp_in,
+                          const void *ln_in, void *lp_out, void *ln_out, double *grad, unsigned int *counter,
+                          int *status, double *partials, int64_t max_blocks, cudaStream_t st, bool accumulate);
 int adjoint_accumulate_end(const pic_grid *g, void *ws, double *grad, cudaStream_t st);
+
+// Binomial checkpointing (revolve.cu).
+int revolve_plan(int64_t n_steps, int64_t n_slots, int64_t *recompute_steps, int64_t *spine_levels);
+int revolve_spine(int64_t n_steps, int64_t n_slots, int64_t *steps, int64_t cap, int64_t *n_levels);
+int revolve_trace(int64_t n_steps, int64_t n_slots, int64_t *events, int64_t cap, int64_t *n_events,
+                  int64_t *advanced);
+int revolve_forward(const pic_grid *g, void *pos0, void *neg0, void *pos1, void *neg1, int64_t n_steps,
+                    const double *xs, const double *ys, const int64_t *off, void *dens, uint32_t *counts,
+                    double *tally, void *slots_pos, void *slots_neg, int64_t state_stride, int64_t n_slots, void *ws,
+                    cudaStream_t st);
+int revolve_backward(const pic_grid *g, void *slots_pos, void *slots_neg, int64_t state_stride, int64_t n_slots,
+                     int64_t n_steps, const double *xs, const double *ys, const int64_t *off, void *dens,
+                     void *work_pos0, void *work_neg0, void *work_pos1, void *work_neg1, void *lam_pos0,
+                     void *lam_neg0, void *lam_pos1, void *lam_neg1, double *grad, void *ws, void *adj_ws,
+                     cudaStream_t st);
 
 int sample_disc(const double *u, int64_t n_pairs, double scale, double mid, double radius_sq, int64_t n_wanted,
                 double *xs, double *ys, int64_t *n_accepted, int64_t *n_pairs_used);
