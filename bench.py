@@ -315,14 +315,15 @@ def run_adjoint_full(args):
     desc, cfg = _config(args.adjoint_workload)
     n = int(args.adjoint_steps)
     limit = float(args.memory_limit_gb) * 1e9
+    shape = None if args.variant == "auto" else {"variant": args.variant}
     for _ in range(max(1, args.warmup)):
-        adj.ks_and_gradient(cfg, max_steps=min(n, 8), memory_limit=limit)
+        adj.ks_and_gradient(cfg, max_steps=min(n, 8), memory_limit=limit, shape=shape)
         torch.cuda.empty_cache()
     runs, plain = [], []
     for _ in range(max(1, args.steps)):
         torch.cuda.synchronize()
         t = time.perf_counter()
-        res = pkg.run_simulation_b200(cfg, progress=False, return_fields=False, max_steps=n)
+        res = pkg.run_simulation_b200(cfg, progress=False, return_fields=False, max_steps=n, shape=shape)
         torch.cuda.synchronize()
         plain.append(time.perf_counter() - t)
         del res
@@ -330,7 +331,7 @@ def run_adjoint_full(args):
         torch.cuda.reset_peak_memory_stats()
         base = torch.cuda.memory_allocated()
         t = time.perf_counter()
-        ks, grad, tm = adj.ks_and_gradient(cfg, max_steps=n, memory_limit=limit)
+        ks, grad, tm = adj.ks_and_gradient(cfg, max_steps=n, memory_limit=limit, shape=shape)
         torch.cuda.synchronize()
         tm["total_s"] = time.perf_counter() - t
         tm["peak_bytes"] = torch.cuda.max_memory_allocated() - base

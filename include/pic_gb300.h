@@ -68,6 +68,11 @@ typedef struct pic_grid {
     int32_t stages;          /* stream variant: shared-memory ring stages    */
     int32_t consumer_warps;  /* stream variant: compute warps per CTA        */
     int32_t ctas_per_sm;     /* stream variant: resident CTAs per SM         */
+    /* Adjoint step kernel (pic_adjoint_*, pic_revolve_backward): a
+     * PIC_VARIANT_* of its own, so tuning the step's shape leaves it alone.
+     * AUTO: STREAM for float32 grids with no_xy >= 4 and no_xy^2 * kpitch >=
+     * 2^24 cells, FLAT otherwise; STREAM on a float64 grid is refused. */
+    int32_t adjoint_variant;
 } pic_grid;
 
 /* Fused-step kernels. FLAT: one thread per four k of a column, neighbours

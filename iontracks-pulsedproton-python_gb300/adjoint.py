@@ -119,8 +119,9 @@ class AdjointRun:
     tallies so far, as ``1 / f_t`` at its last step). ``slots``: the binomial
     schedule's state slots (default: as many as the memory limit allows, at
     most one per step). ``shape``: launch shape of the step kernels
-    (``{"variant": "flat" | "stream", ...}``; the adjoint follows the
-    variant), default the library's choice for the grid.
+    (``{"variant": "flat" | "stream", ..., "adjoint_variant": ...}``);
+    default: the autotuned step shape (as :func:`run_simulation_b200`) and the
+    library's choice of adjoint kernel for the grid.
     """
 
     def __init__(self, config, theta=None, checkpoint_every: int = 64, dtype: str = "float32", rng=None,
@@ -205,6 +206,10 @@ class AdjointRun:
         np.cumsum(schedule, out=self.offsets[1:])
         eng = ChamberEngine(cfg, dtype=self.dtype, max_tracks=max(1, n_tracks), tally_steps=max(total, 1),
                             shape=self.shape)
+        if self.shape is None:
+            from .autotune import tune
+
+            tune(eng, quick=True)  # on the fresh (zero) fields: leaves them zero
         (pl, pzm, pzp, pc), (nl, nzm, nzp, nc), adt, _ = _weights(cfg, self.theta)
         g = eng.grid
         g.p_lat, g.p_zm, g.p_zp, g.p_cen = pl, pzm, pzp, pc

@@ -447,11 +447,9 @@ int tile_rows(int n, int kp) {
 
 bool adjoint_stream_eligible(const pic_grid *g) {
     if (g->dtype != PIC_F32 || g->no_xy < 4 || g->no_xy > 16383) return false;
-    int variant = g->variant;
-    if (variant == PIC_VARIANT_AUTO)
-        variant = (g->no_xy >= 64 && g->no_xy * g->no_xy * g->kpitch >= kStreamMinCells) ? PIC_VARIANT_STREAM
-                                                                                          : PIC_VARIANT_FLAT;
-    return variant == PIC_VARIANT_STREAM && tile_rows((int)g->no_xy, (int)g->kpitch) >= 1;
+    if (tile_rows((int)g->no_xy, (int)g->kpitch) < 1) return false;
+    if (g->adjoint_variant == PIC_VARIANT_AUTO) return g->no_xy * g->no_xy * g->kpitch >= kAdjStreamMinCells;
+    return g->adjoint_variant == PIC_VARIANT_STREAM;
 }
 
 int launch_adjoint_stream(const pic_grid *g, const void *pos, const void *neg, const void *dens, const void *lp_in,

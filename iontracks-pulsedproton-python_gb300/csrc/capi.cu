@@ -152,6 +152,11 @@ static int check_grid(const pic_grid *g) {
     if (g->no_xy > (int64_t)1 << 20 || g->nzb > (int64_t)1 << 20)
         return set_error(PIC_E_CAPACITY, "grid extent beyond 2^20 voxels per axis");
     if (!(g->cutoff_voxels > 0.0)) return set_error(PIC_E_INVALID, "cutoff_voxels must be positive");
+    if (g->adjoint_variant != PIC_VARIANT_AUTO && g->adjoint_variant != PIC_VARIANT_FLAT &&
+        g->adjoint_variant != PIC_VARIANT_STREAM)
+        return set_error(PIC_E_INVALID, "adjoint_variant must be PIC_VARIANT_AUTO, _FLAT or _STREAM");
+    if (g->adjoint_variant == PIC_VARIANT_STREAM && g->dtype != PIC_F32)
+        return set_error(PIC_E_INVALID, "the stream adjoint variant supports float32 fields only");
     ScoreTest t;
     return score_test(g, &t);
 }
@@ -234,7 +239,7 @@ extern "C" {
 
 const char *pic_last_error(void) { return g_last_error.c_str(); }
 
-int pic_abi_version(void) { return 2; }
+int pic_abi_version(void) { return 3; }
 
 int64_t pic_kpitch(int64_t nzb) { return (nzb + 7) / 8 * 8; }
 

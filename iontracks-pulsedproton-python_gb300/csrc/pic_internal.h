@@ -134,8 +134,10 @@ int adjoint_workspace_bytes(int64_t *bytes);
 int launch_adjoint(const pic_grid *g, const void *pos, const void *neg, const void *dens, void *lp_in, void *ln_in,
                    void *lp_out, void *ln_out, double *grad, void *ws, cudaStream_t st, bool accumulate = false);
 int adjoint_accumulate_begin(const pic_grid *g, void *ws, cudaStream_t st);
-// The streaming adjoint (adjoint_stream.cu): float32 grids that run the
-// streaming forward step (variant STREAM, or AUTO at kStreamMinCells cells).
+// The streaming adjoint (adjoint_stream.cu): float32 grids with
+// adjoint_variant STREAM, or AUTO and at least kAdjStreamMinCells cells (the
+// grid no longer fits L2 and the flat kernel waits on its neighbour loads).
+constexpr int64_t kAdjStreamMinCells = (int64_t)1 << 24;
 bool adjoint_stream_eligible(const pic_grid *g);
 int launch_adjoint_stream(const pic_grid *g, const void *pos, const void *neg, const void *dens, const void *lp_in,
                           const void *ln_in, void *lp_out, void *ln_out, double *grad, unsigned int *counter,

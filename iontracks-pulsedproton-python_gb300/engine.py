@@ -26,9 +26,9 @@ def apply_shape(g: N.PicGrid, shape: dict | None) -> N.PicGrid:
     """Sets launch-shape fields of a descriptor from a dict (``variant`` may
     be ``"auto"``, ``"flat"`` or ``"stream"``); unknown keys raise."""
     for key, val in (shape or {}).items():
-        if key not in SHAPE_FIELDS:
-            raise ValueError(f"unknown launch-shape field {key!r}; expected one of {SHAPE_FIELDS}")
-        if key == "variant" and isinstance(val, str):
+        if key not in SHAPE_FIELDS + ("adjoint_variant",):
+            raise ValueError(f"unknown launch-shape field {key!r}; expected one of {SHAPE_FIELDS + ('adjoint_variant',)}")
+        if key in ("variant", "adjoint_variant") and isinstance(val, str):
             if val not in _VARIANTS:
                 raise ValueError(f"variant must be one of {sorted(_VARIANTS)}, got {val!r}")
             val = _VARIANTS[val]

@@ -344,8 +344,8 @@ def _adjoint_step(g, pos, neg, dens, lp, ln):
 @pytest.mark.parametrize("wall", ["absorbing", "reflecting"])
 @pytest.mark.parametrize("deposit", [False, True])
 def test_stream_adjoint_step_equals_the_flat_one(wall, deposit):
-    """pic_adjoint_step with the streaming kernel (variant STREAM) against the
-    flat kernel (variant FLAT) on the same random state, lambda and
+    """pic_adjoint_step with the streaming kernel (adjoint_variant STREAM)
+    against the flat kernel (adjoint_variant FLAT) on the same random state, lambda and
     deposition pairs, on a grid whose tiles and work items are ragged (the
     10 um chamber at r = 0.035 cm): lambda_s of every column, the ring's
     included, to 1e-6 of its scale; the step's five derivative sums to 1e-5
@@ -374,7 +374,7 @@ def test_stream_adjoint_step_equals_the_flat_one(wall, deposit):
     out = {}
     for variant in (N.PIC_VARIANT_FLAT, N.PIC_VARIANT_STREAM):
         g = eng_mod.make_grid(cfg, "float32")
-        g.variant = variant
+        g.adjoint_variant = variant
         out[variant] = _adjoint_step(g, pos, neg, dens, lp, ln)
     f, s = out[N.PIC_VARIANT_FLAT], out[N.PIC_VARIANT_STREAM]
     assert s[3] == 0 and np.all(np.isfinite(s[0])) and np.all(np.isfinite(s[1]))
@@ -392,7 +392,8 @@ def test_stream_variant_gradient(wall):
     to 1e-5 relative per parameter."""
     A = _adj()
     cfg = make_config("column_10um_r02", sampled_radius_cm=0.035, lateral_boundary=wall)
-    ks0, g0, _ = A.ks_and_gradient(cfg, None, dtype="float32", shape={"variant": "flat"})
-    ks1, g1, _ = A.ks_and_gradient(cfg, None, dtype="float32", shape={"variant": "stream"})
+    ks0, g0, _ = A.ks_and_gradient(cfg, None, dtype="float32", shape={"variant": "flat", "adjoint_variant": "flat"})
+    ks1, g1, _ = A.ks_and_gradient(cfg, None, dtype="float32",
+                                   shape={"variant": "stream", "adjoint_variant": "stream"})
     assert abs(ks1 - ks0) <= 1e-6
     np.testing.assert_allclose(g1, g0, rtol=1e-5)

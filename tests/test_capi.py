@@ -57,7 +57,7 @@ def test_binding_covers_the_header(lib):
 
 
 def test_host_only_calls_without_a_gpu(lib):
-    assert lib.pic_abi_version() == 2
+    assert lib.pic_abi_version() == 3
     assert lib.pic_kpitch(406) == 408
     assert lib.pic_kpitch(408) == 408
     assert lib.pic_kpitch(3) == 8
