@@ -40,6 +40,11 @@ BLOCKS_PER_SM = 3
 WAVES = 4
 MIN_ITEMS_PER_BLOCK = 256
 MAX_ITEMS_PER_BLOCK = 1 << 16
+# Phases with at most this many active grids step each grid alone with the
+# single-grid kernels (pic_run_segment on its slices of the packed buffers):
+# there the batched launch is bound by its per-block table and reduction work
+# (23 us a step for one 53 x 53 x 208 grid), the flat step kernel is not.
+SOLO_MAX_GRIDS = 2
 
 
 def items_per_block(total_items: int, sms: int) -> int:
@@ -143,6 +148,7 @@ def run_batched_b200(
     chunk_steps: int = 512,
     progress: bool = False,
     persistent: bool = False,
+    solo_grids: int = SOLO_MAX_GRIDS,
 ):
     """Simulate every configuration and return their Results, in order.
 
@@ -154,6 +160,8 @@ def run_batched_b200(
     step is two launches (``pic_batched_segment``). Measured on GB300 over the
     64-configuration sweep the per-step launches are faster (1.31 vs 1.44 s):
     two device-wide barriers per step cost what two launch gaps do.
+    Phases with at most ``solo_grids`` active grids run each grid's chunk
+    with the single-grid kernels instead (0: never).
     """
     import torch
 
@@ -264,6 +272,7 @@ def run_batched_b200(
         i0, i1 = b * it // nbr, (b + 1) * it // nbr
         max_blocks = max(max_blocks, len(blk_cfg))
         phases.append((s0, s1, dict(
+            active=[int(c) for c in act],
             blk_cfg=torch.from_numpy(blk_cfg.astype(np.int32)).to(dev),
             blk_item0=torch.from_numpy(i0).to(dev),
             blk_item1=torch.from_numpy(i1).to(dev),
@@ -278,6 +287,27 @@ def run_batched_b200(
     workspace = torch.zeros(int(wsb.value), dtype=torch.uint8, device=dev)
 
     st = torch.cuda.current_stream(dev).cuda_stream
+    solo_ws = None
+    if solo_grids > 0 and not persistent and any(len(t["active"]) <= solo_grids for _, _, t in phases):
+        swb = ctypes.c_int64()
+        N.check(lib.pic_step_workspace_bytes(ctypes.byref(grids[0]), ctypes.byref(swb)), "pic_step_workspace_bytes")
+        solo_ws = torch.zeros(int(swb.value), dtype=torch.uint8, device=dev)
+
+    def run_solo(c, c0, c1):
+        """Grid c's global steps [c0, c1) with the single-grid kernels, on its
+        slices: state of step s in buffer s & 1, deposition pairs in buffer
+        s & 1 (the batched step clears the other one every step, as
+        pic_run_segment expects), tallies at row tally_off + s."""
+        fo, do2 = field_off[c] * es, 2 * dens_off[c] * es
+        off = np.ascontiguousarray(offsets[c][c0 : c1 + 1])
+        N.check(lib.pic_run_segment(
+            ctypes.byref(grids[c]), pos[0].data_ptr() + fo, neg[0].data_ptr() + fo, pos[1].data_ptr() + fo,
+            neg[1].data_ptr() + fo, c0 & 1, c1 - c0, xs_dev.data_ptr() + 8 * track_base[c],
+            ys_dev.data_ptr() + 8 * track_base[c], off.ctypes.data, dens[0].data_ptr() + do2,
+            dens[1].data_ptr() + do2, c0 & 1, counts.data_ptr() + 4 * counts_off[c],
+            tally.data_ptr() + 32 * (tally_off[c] + c0), solo_ws.data_ptr(), solo_ws.numel(), st),
+            "pic_run_segment")
+
     sto_dev = torch.from_numpy(step_task_off).to(dev)
     stt_dev = torch.from_numpy(np.ascontiguousarray(step_tracks, dtype=np.int64)).to(dev)
     # chunks of global steps; chunk (c0, c1) needs grid c's tracks
@@ -299,6 +329,12 @@ def run_batched_b200(
             feeder.upload(pending, xs_dev, ys_dev)
             # draw the next chunk's tracks while the device runs this one
             pending = feeder.submit(jobs_of(*chunks[k + 1][:2])) if k + 1 < len(chunks) else None
+            if solo_ws is not None and len(tab["active"]) <= solo_grids:
+                for c in tab["active"]:  # independent grids: one after the other
+                    run_solo(c, c0, c1)
+                if progress:
+                    print(f"  global step {c1}/{S}")
+                continue
             L = PicBatchLaunch()
             L.cfgs = cfg_dev.data_ptr()
             L.n_cfgs = n_cfg
@@ -330,6 +366,12 @@ def run_batched_b200(
             if progress:
                 print(f"  global step {c1}/{S}")
         torch.cuda.synchronize(dev)
+        if solo_ws is not None:
+            sv = ctypes.c_int32()
+            N.check(lib.pic_workspace_status(solo_ws.data_ptr(), 1, st, ctypes.byref(sv)), "pic_workspace_status")
+            if sv.value != 0:
+                raise RuntimeError(f"a fused-step kernel gave up on a bounded wait (code {sv.value}); "
+                                   "results are invalid")
         if persistent and chunks:
             status = ctypes.c_int32()
             N.check(lib.pic_batched_status(ctypes.byref(L), st, ctypes.byref(status)), "pic_batched_status")

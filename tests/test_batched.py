@@ -110,3 +110,26 @@ def test_persistent_launch_matches_per_step_launches(dtype):
         assert abs(x.ks - y.ks) <= tol
         np.testing.assert_allclose(y.recombination, x.recombination, rtol=0,
                                    atol=tol * max(np.abs(x.recombination).max(), 1e-300))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype", ["float32", "float64"])
+def test_single_grid_phases_match_batched_launches(dtype):
+    """Phases stepped grid by grid with the single-grid kernels (on the
+    grids' slices of the packed buffers) against batched launches: no phase
+    (solo_grids=0), the default (phases of at most two grids), and every
+    phase; chunks of 7 steps hand the state over between the two paths many
+    times. Identical tracks, k_s, tallies and fields to the dtype's rounding."""
+    cfgs = _mixed_batch()
+    runs = [pkg().run_batched_b200(cfgs, dtype=dtype, chunk_steps=7, solo_grids=k, return_fields=True)
+            for k in (0, 2, len(cfgs))]
+    tol = 1e-5 if dtype == "float32" else 1e-12
+    for other in runs[1:]:
+        for x, y in zip(runs[0], other):
+            np.testing.assert_array_equal(x.track_density_xy, y.track_density_xy)
+            assert abs(x.ks - y.ks) <= tol
+            np.testing.assert_allclose(y.recombination, x.recombination, rtol=0,
+                                       atol=tol * max(np.abs(x.recombination).max(), 1e-300))
+            peak = max(np.abs(x.positive_array).max(), 1e-300)
+            np.testing.assert_allclose(y.positive_array, x.positive_array, rtol=0, atol=tol * peak)
+            np.testing.assert_allclose(y.negative_array, x.negative_array, rtol=0, atol=tol * peak)
