@@ -68,6 +68,11 @@ typedef struct pic_grid {
     int32_t stages;          /* stream variant: shared-memory ring stages    */
     int32_t consumer_warps;  /* stream variant: compute warps per CTA        */
     int32_t ctas_per_sm;     /* stream variant: resident CTAs per SM         */
+    int32_t steps_per_launch; /* flat variant: 0 or 1 = one launch per step
+                              * (two with tracks); K in 2 .. 256 = up to K
+                              * steps per cooperative launch (device-wide
+                              * barriers between the phases of a step), for
+                              * latency-bound small grids */
     /* Adjoint step kernel (pic_adjoint_*, pic_revolve_backward): a
      * PIC_VARIANT_* of its own, so tuning the step's shape leaves it alone.
      * AUTO: STREAM for float32 grids with no_xy >= 4 and no_xy^2 * kpitch >=

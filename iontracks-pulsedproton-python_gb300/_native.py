@@ -60,6 +60,7 @@ class PicGrid(ctypes.Structure):
         ("stages", ctypes.c_int32),
         ("consumer_warps", ctypes.c_int32),
         ("ctas_per_sm", ctypes.c_int32),
+        ("steps_per_launch", ctypes.c_int32),
         ("adjoint_variant", ctypes.c_int32),
     ]
 

@@ -21,6 +21,7 @@
 
 #include "pic_deposit.cuh"
 #include "pic_device.cuh"
+#include "pic_barrier.cuh"
 #include "pic_flat.cuh"
 #include "pic_internal.h"
 
@@ -265,45 +266,7 @@ static int prep_table(const BatchLaunch &L, cudaStream_t st) {
     return check_launch("batched_prep_kernel");
 }
 
-// Device-wide barrier of a cooperative launch (every block resident). The
-// last block to arrive resets the count and opens the barrier; the others wait
-// for that, a bounded number of polls: a wait that runs out sets the status
-// word and every block leaves at its next barrier (the host then reads the
-// status). Returns false when the kernel must stop.
-constexpr long long kBarrierPolls = 1LL << 24;  // x ~100 ns: a few seconds
-
-__device__ bool grid_barrier(GridBarrier *bar) {
-    __shared__ int ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile GridBarrier *vb = bar;
-        const unsigned int g = vb->gen;
-        __threadfence();  // this block's writes before its arrival
-        ok = 1;
-        if (atomicAdd(&bar->count, 1u) == gridDim.x - 1) {
-            atomicExch(&bar->count, 0u);
-            __threadfence();
-            atomicAdd(&bar->gen, 1u);
-        } else {
-            long long polls = 0;
-            while (vb->gen == g) {
-                if (vb->status != 0) {
-                    ok = 0;
-                    break;
-                }
-                if (++polls > kBarrierPolls) {
-                    atomicCAS(&bar->status, 0, 5);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(100);
-            }
-        }
-        __threadfence();  // the other blocks' writes before this block reads
-    }
-    __syncthreads();
-    return ok != 0;
-}
+__device__ __forceinline__ BarrierRef barrier_ref(GridBarrier *b) { return BarrierRef{&b->count, &b->gen, &b->status}; }
 
 template <typename T>
 struct BatchPersistArgs {
@@ -338,7 +301,7 @@ __global__ void __launch_bounds__(256) batched_persistent_kernel(BatchPersistArg
                 batched_deposit_warp<T>(p.b.cfgs, p.task_cfg + t0, p.task_first + t0, p.task_prefix + t0,
                                         (int)(t1 - t0), w / parts, p.xs, p.ys, (pair_t<T> *)p.dens[bi], p.counts,
                                         lane, (int)(w % parts), parts);
-            if (!grid_barrier(p.bar)) return;
+            if (!grid_barrier(barrier_ref(p.bar))) return;
         }
         BatchStepArgs<T> b = p.b;
         b.pos_in = (const T *)p.pos[bi];
@@ -352,7 +315,7 @@ __global__ void __launch_bounds__(256) batched_persistent_kernel(BatchPersistArg
             __syncthreads();  // shared staging of the previous entry is done with
             batched_step_block<T, BLOCK, I, true>(b, vb, red, last, a);
         }
-        if (!grid_barrier(p.bar)) return;
+        if (!grid_barrier(barrier_ref(p.bar))) return;
     }
 }
 

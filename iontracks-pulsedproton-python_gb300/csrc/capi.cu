@@ -152,6 +152,8 @@ static int check_grid(const pic_grid *g) {
     if (g->no_xy > (int64_t)1 << 20 || g->nzb > (int64_t)1 << 20)
         return set_error(PIC_E_CAPACITY, "grid extent beyond 2^20 voxels per axis");
     if (!(g->cutoff_voxels > 0.0)) return set_error(PIC_E_INVALID, "cutoff_voxels must be positive");
+    if (g->steps_per_launch < 0 || g->steps_per_launch > kMaxMultiSteps)
+        return set_error(PIC_E_INVALID, "steps_per_launch must be 0 .. 256");
     if (g->adjoint_variant != PIC_VARIANT_AUTO && g->adjoint_variant != PIC_VARIANT_FLAT &&
         g->adjoint_variant != PIC_VARIANT_STREAM)
         return set_error(PIC_E_INVALID, "adjoint_variant must be PIC_VARIANT_AUTO, _FLAT or _STREAM");
@@ -175,6 +177,23 @@ static int run_loop(const pic_grid *g, void *pos0, void *neg0, void *pos1, void 
                     void *dens1, int64_t dens_parity, uint32_t *counts, double *tally, void *ws,
                     cudaStream_t st) {
     void *pos[2] = {pos0, pos1}, *neg[2] = {neg0, neg1}, *dens[2] = {dens0, dens1};
+    pic_grid r = *g;
+    int rc0 = resolve_shape(&r);
+    if (rc0) return rc0;
+    if (multistep_eligible(&r)) {
+        // up to steps_per_launch steps per cooperative launch
+        const int64_t K = r.steps_per_launch;
+        unsigned int *bar = workspace_layout(ws).counter + 16;
+        for (int64_t s0 = 0; s0 < n_steps; s0 += K) {
+            const int64_t m = n_steps - s0 < K ? n_steps - s0 : K;
+            cudaError_t e = cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned int), st);
+            if (e != cudaSuccess) return set_cuda_error("cudaMemsetAsync(barrier)", e);
+            int rc = launch_multistep(&r, pos, neg, (int)((parity + s0) & 1), (int)m, xs, ys, off + s0, dens,
+                                      (int)((dens_parity + s0) & 1), counts, tally + 4 * s0, ws, st);
+            if (rc) return rc;
+        }
+        return PIC_OK;
+    }
     for (int64_t s = 0; s < n_steps; ++s) {
         const int bi = (int)((parity + s) & 1), bo = bi ^ 1;
         const int di = (int)((dens_parity + s) & 1);
@@ -239,7 +258,7 @@ extern "C" {
 
 const char *pic_last_error(void) { return g_last_error.c_str(); }
 
-int pic_abi_version(void) { return 3; }
+int pic_abi_version(void) { return 4; }
 
 int64_t pic_kpitch(int64_t nzb) { return (nzb + 7) / 8 * 8; }
 

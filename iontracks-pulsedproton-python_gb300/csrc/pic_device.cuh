@@ -29,16 +29,17 @@ __device__ __forceinline__ V4<double> load4(const double *p) {
     double2 b = __ldg(reinterpret_cast<const double2 *>(p) + 1);
     return {{a.x, a.y, b.x, b.y}};
 }
-// Coherent forms (plain global loads) for kernels that read data written
-// earlier in the same launch by other blocks (the persistent batched kernel):
-// the read-only path of __ldg is not kept coherent with such writes.
+// Coherent forms for kernels that read data written earlier in the same
+// launch by other blocks (the persistent kernels): loads cached in L2 only
+// (ld.global.cg). Neither the read-only path of __ldg nor an SM's L1 is kept
+// coherent with other SMs' writes; L2 is the point of coherence.
 __device__ __forceinline__ V4<float> load4c(const float *p) {
-    const float4 t = *reinterpret_cast<const float4 *>(p);
+    const float4 t = __ldcg(reinterpret_cast<const float4 *>(p));
     return {{t.x, t.y, t.z, t.w}};
 }
 __device__ __forceinline__ V4<double> load4c(const double *p) {
-    const double2 a = reinterpret_cast<const double2 *>(p)[0];
-    const double2 b = reinterpret_cast<const double2 *>(p)[1];
+    const double2 a = __ldcg(reinterpret_cast<const double2 *>(p));
+    const double2 b = __ldcg(reinterpret_cast<const double2 *>(p) + 1);
     return {{a.x, a.y, b.x, b.y}};
 }
 __device__ __forceinline__ void store4(float *p, const V4<float> &v) {

@@ -29,9 +29,16 @@ struct StepArgs {
     FastDiv div_c4, div_n;  // item -> column -> (i, j) on the 32-bit path
 };
 
-template <typename T>
+// One element or one deposition pair: plain, or (COH) from L2 only.
+template <bool COH, typename V>
+__device__ __forceinline__ V ld1(const V *p) {
+    if constexpr (COH) return __ldcg(p);
+    else return *p;
+}
+
+template <typename T, bool COH = false>
 __device__ __forceinline__ T dep_at(const StepArgs<T> &a, int64_t dcol) {
-    return a.dens ? a.dens[dcol].x : T(0);
+    return a.dens ? ld1<COH>(a.dens + dcol).x : T(0);
 }
 
 // Index type of a grid: 32-bit unsigned offsets when every element offset of
@@ -89,7 +96,7 @@ __device__ __forceinline__ void flat_item(const StepArgs<T> &a, I item, Tally<T>
     const I out_off = col * kp + k0;
 
     if (ring && !a.reflecting) {
-        const T d = dep_at(a, (int64_t)(i * dp + j));
+        const T d = dep_at<T, COH>(a, (int64_t)(i * dp + j));
         V4<T> P = ld4(a.pos_in + out_off), N = ld4(a.neg_in + out_off);
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
@@ -109,17 +116,17 @@ __device__ __forceinline__ void flat_item(const StepArgs<T> &a, I item, Tally<T>
     V4<T> Pjm = ld4(a.pos_in + base - kp), Pjp = ld4(a.pos_in + base + kp);
     V4<T> Nim = ld4(a.neg_in + base - di), Nip = ld4(a.neg_in + base + di);
     V4<T> Njm = ld4(a.neg_in + base - kp), Njp = ld4(a.neg_in + base + kp);
-    T pkm = c > 0 ? a.pos_in[base - 1] : T(0);
-    T nkm = c > 0 ? a.neg_in[base - 1] : T(0);
-    T pkp = k0 + 4 < kp ? a.pos_in[base + 4] : T(0);
-    T nkp = k0 + 4 < kp ? a.neg_in[base + 4] : T(0);
+    T pkm = c > 0 ? ld1<COH>(a.pos_in + base - 1) : T(0);
+    T nkm = c > 0 ? ld1<COH>(a.neg_in + base - 1) : T(0);
+    T pkp = k0 + 4 < kp ? ld1<COH>(a.pos_in + base + 4) : T(0);
+    T nkp = k0 + 4 < kp ? ld1<COH>(a.neg_in + base + 4) : T(0);
 
     const I dcol = ci * dp + cj;
     // this column's deposition and its neighbours' (gap layers only): one
     // pair per column
     T dc = T(0), dl = T(0);
     if (a.dens) {
-        const pair_t<T> d = a.dens[dcol];
+        const pair_t<T> d = ld1<COH>(a.dens + dcol);
         dc = d.x;
         dl = d.y;
 #pragma unroll

@@ -126,6 +126,14 @@ int batched_persistent(const BatchLaunch &L, const int64_t *step_task_off, const
                        cudaStream_t st);
 int batched_status(const BatchLaunch &L, cudaStream_t st, int32_t *status);
 
+// Several steps of one grid per cooperative launch (multistep.cu): for a
+// resolved FLAT grid with steps_per_launch > 1.
+constexpr int kMaxMultiSteps = 256;
+bool multistep_eligible(const pic_grid *resolved);
+int launch_multistep(const pic_grid *g, void *const pos[2], void *const neg[2], int parity, int n_steps,
+                     const double *xs, const double *ys, const int64_t *off, void *const dens[2], int dens_parity,
+                     uint32_t *counts, double *tally, void *ws, cudaStream_t st);
+
 int step_noalloc(const pic_grid *g, const void *pos_in, const void *neg_in, void *pos_out, void *neg_out,
                  const double *xs, const double *ys, int64_t n_tracks, uint32_t *counts, double *tally,
                  cudaStream_t st);

@@ -19,7 +19,7 @@ from .constants import RECOMBINATION_ALPHA_CM3_S
 
 _DTYPES = {"float32": N.PIC_F32, "float64": N.PIC_F64}
 _VARIANTS = {"auto": N.PIC_VARIANT_AUTO, "flat": N.PIC_VARIANT_FLAT, "stream": N.PIC_VARIANT_STREAM}
-SHAPE_FIELDS = ("variant", "tile_rows", "planes_per_item", "stages", "consumer_warps", "ctas_per_sm")
+SHAPE_FIELDS = ("variant", "tile_rows", "planes_per_item", "stages", "consumer_warps", "ctas_per_sm", "steps_per_launch")
 
 
 def apply_shape(g: N.PicGrid, shape: dict | None) -> N.PicGrid:

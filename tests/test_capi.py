@@ -57,7 +57,7 @@ def test_binding_covers_the_header(lib):
 
 
 def test_host_only_calls_without_a_gpu(lib):
-    assert lib.pic_abi_version() == 3
+    assert lib.pic_abi_version() == 4
     assert lib.pic_kpitch(406) == 408
     assert lib.pic_kpitch(408) == 408
     assert lib.pic_kpitch(3) == 8
@@ -87,6 +87,10 @@ def test_invalid_grid_is_refused_before_any_device_work(lib):
     g.mid_xy, g.scoring_radius_sq = 4.0, 0.0
     assert lib.pic_step_workspace_bytes(ctypes.byref(g), ctypes.byref(b)) == native.PIC_E_INVALID
     g.scoring_radius_sq = 9.0
+    g.steps_per_launch = 257
+    assert lib.pic_step_workspace_bytes(ctypes.byref(g), ctypes.byref(b)) == native.PIC_E_INVALID
+    assert b"steps_per_launch" in lib.pic_last_error()
+    g.steps_per_launch = 256
     assert lib.pic_step_workspace_bytes(ctypes.byref(g), ctypes.byref(b)) == native.PIC_OK
     assert b.value > 0
     rc = lib.pic_step(ctypes.byref(g), None, None, None, None, None, None, None, None, 0, None)

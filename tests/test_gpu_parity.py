@@ -220,6 +220,40 @@ def test_stream_variant_matches_reference(name, shape):
         np.testing.assert_allclose(res.negative_array, fx["negative_array"], rtol=0, atol=peak * 1e-5)
 
 
+MULTI_SHAPES = {"two": 2, "seven": 7, "max": 256}
+
+
+@pytest.mark.parametrize("graphs", [False, True])
+@pytest.mark.parametrize("spl", sorted(MULTI_SHAPES))
+@pytest.mark.parametrize("name", STREAM_RUNS)
+def test_multistep_launches_match_reference(name, spl, graphs):
+    """Several steps per cooperative launch (steps_per_launch 2, 7 and 256:
+    launches that end inside pulses and idle stretches, with and without
+    CUDA graphs) against the reference fixtures, float32."""
+    cfg, fx = run_config(name)
+    res = _solver()(cfg, progress=False, use_graphs=graphs,
+                    shape={"variant": "flat", "steps_per_launch": MULTI_SHAPES[spl]})
+    _check_f32(res, float(fx["ks"]), fx["injected"], fx["recombination"], fx["n_positive"], fx["n_negative"],
+               fx["track_density_xy"])
+    if "positive_array" in fx:
+        peak = np.abs(fx["positive_array"]).max()
+        np.testing.assert_allclose(res.positive_array, fx["positive_array"], rtol=0, atol=peak * 1e-5)
+        np.testing.assert_allclose(res.negative_array, fx["negative_array"], rtol=0, atol=peak * 1e-5)
+
+
+@pytest.mark.parametrize("wall", ["absorbing", "reflecting"])
+def test_multistep_float64_matches_the_oracle(oracle, wall):
+    """Float64 fields, 5 steps per launch: k_s and the recombined tally per
+    step equal the float64 oracle's to 1e-10; the tracks are identical."""
+    cfg = make_config("fast_dense", lateral_boundary=wall, n_pulses=3, repetition_rate_hz=20000.0)
+    res = _solver()(cfg, progress=False, dtype="float64", shape={"variant": "flat", "steps_per_launch": 5})
+    ref = oracle.run(cfg, mode="batched", threads=2)
+    np.testing.assert_array_equal(res.track_density_xy, ref["track_density_xy"])
+    assert res.ks == pytest.approx(ref["ks"], rel=1e-10)
+    np.testing.assert_allclose(res.recombination, ref["recombined"], rtol=1e-10,
+                               atol=1e-10 * np.abs(ref["recombined"]).max())
+
+
 @pytest.mark.parametrize("wall", ["absorbing", "reflecting"])
 def test_stream_and_flat_agree_on_a_large_grid(wall):
     """208 x 208 x 406 (5 um, r = 0.05 cm), 40 steps of the pulse at 89.1 Gy/s
@@ -348,3 +382,22 @@ def test_plain_method_at_scale_matches_the_oracle(oracle):
     np.testing.assert_array_equal(res.track_density_xy, ref["track_density_xy"])
     assert abs(res.ks - ref["ks"]) <= KS_ABS
     assert res.recombination.sum() == pytest.approx(ref["recombined"].sum(), rel=TALLY_REL)
+
+
+def test_autotuner_chooses_steps_per_launch():
+    """The autotuner times a flat float32 grid's idle steps as one CUDA graph
+    of per-step launches and as cooperative launches of 32 and 256 steps, and
+    keeps the fastest; the run with its choice matches the reference."""
+    eng_mod = importlib.import_module(pkg().__name__ + ".engine")
+    at = importlib.import_module(pkg().__name__ + ".autotune")
+    cfg, fx = run_config("run_fast_dense")
+    eng = eng_mod.ChamberEngine(cfg, dtype="float32")
+    best = at.tune(eng, quick=True, reps=3, use_cache=False)
+    tried = dict(best["steps_per_launch"])
+    assert sorted(tried) == [0, 32, 256] and all(ms > 0 for ms in tried.values())
+    chosen = best["shape"].get("steps_per_launch", 0)
+    assert tried[chosen] == min(tried.values())
+    eng.close()
+    res = _solver()(cfg, progress=False, shape=best["shape"])
+    _check_f32(res, float(fx["ks"]), fx["injected"], fx["recombination"], fx["n_positive"], fx["n_negative"],
+               fx["track_density_xy"])
