@@ -44,8 +44,8 @@ def candidate_shapes(grid, quick: bool = False) -> list[dict]:
         return out
     out.append({"variant": "stream"})  # the library's own default shape
     kp = grid.kpitch
-    tjs = (3, 5, 7, 10, 12) if quick else (2, 3, 4, 5, 6, 7, 8, 10, 12, 14)
-    cws = (8, 12, 16) if quick else (4, 6, 8, 10, 12, 16)
+    tjs = (3, 5, 7, 8, 10, 12, 15) if quick else (2, 3, 4, 5, 6, 7, 8, 10, 12, 14, 15)
+    cws = (8, 12, 13, 15, 16) if quick else (4, 6, 8, 10, 12, 13, 14, 15, 16)
     planes = (4, 16, 64) if quick else (4, 8, 16, 32, 64, 128)
     stage_counts = (4, 5, 6, 8) if quick else (4, 5, 6, 8, 10, 12, 16)
     for tj, cw, ctas, stages, li in itertools.product(tjs, cws, (1, 2), stage_counts, planes):
@@ -55,9 +55,12 @@ def candidate_shapes(grid, quick: bool = False) -> list[dict]:
         if ctas * (smem + 3 * 1024) > _SMEM_PER_SM:
             continue
         ipt = -(-(tj * (kp // 4)) // (cw * 32))
-        if ipt > 6 or (cw + 1) * 32 > (544, 416, 352, 288, 288, 288)[ipt - 1]:
+        # thread limits of the kernel's instantiations (2 to 4 items a thread
+        # also come in wider forms, up to 17 warps, held to fewer registers)
+        threads = (cw + 1) * 32
+        if ipt > 6 or threads > (544, 544, 544, 544, 288, 288)[ipt - 1]:
             continue
-        regs = (96, 128, 152, 168, 168, 168)[ipt - 1]
+        regs = min((96, 128, 152, 168, 168, 168)[ipt - 1], 65536 // (-(-threads // 128) * 128))
         if ctas * (cw + 1) * 32 * regs > 65536:
             continue
         out.append(dict(variant="stream", tile_rows=tj, consumer_warps=cw, ctas_per_sm=ctas, stages=stages,

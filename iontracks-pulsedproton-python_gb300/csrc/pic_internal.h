@@ -37,6 +37,14 @@ constexpr int kStreamMaxThreads = 17 * 32;
 __host__ __device__ constexpr int stream_max_threads(int ipt) {
     return ipt <= 1 ? 17 * 32 : (ipt == 2 ? 13 * 32 : (ipt == 3 ? 11 * 32 : 9 * 32));
 }
+// Wider instantiations for 2 to 4 items a thread allow up to 16 consumer
+// warps: more warps per SM to hide latency, each thread held to fewer
+// registers (65536 / the block rounded up to 128 threads). A launch takes the
+// narrowest instantiation its threads fit.
+constexpr int kStreamWide1 = 16 * 32, kStreamWide2 = 17 * 32;
+__host__ __device__ constexpr int stream_thread_limit(int ipt) {
+    return (ipt >= 2 && ipt <= 4) ? kStreamWide2 : stream_max_threads(ipt);
+}
 // items (k-vectors of a plane) per consumer thread: 1 .. kStreamMaxIpt
 constexpr int kStreamMaxIpt = 6;
 constexpr int kStreamMaxSmem = 227 * 1024;

@@ -103,8 +103,8 @@ __device__ void finish_tally_rt(double (&v)[4], double *partials, unsigned int *
     }
 }
 
-template <int IPT>
-__global__ void __launch_bounds__(stream_max_threads(IPT), 1) stream_step_kernel(StreamArgs a) {
+template <int IPT, int MAXT>
+__global__ void __launch_bounds__(MAXT, 1) stream_step_kernel(StreamArgs a) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ volatile int abort_flag;
     uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw);
@@ -460,17 +460,26 @@ __global__ void __launch_bounds__(stream_max_threads(IPT), 1) stream_step_kernel
     finish_tally_rt(v, a.partials, a.counter, a.tally, a.injected_scale);
 }
 
-template <int IPT>
+template <int IPT, int MAXT = stream_max_threads(IPT)>
 static int launch_ipt(const StreamArgs &a, unsigned blocks, int threads, int smem, cudaStream_t st) {
     static int configured = 0;  // per instantiation: largest dynamic smem set so far
     if (smem > configured) {
         cudaError_t e =
-            cudaFuncSetAttribute(stream_step_kernel<IPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            cudaFuncSetAttribute(stream_step_kernel<IPT, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return set_cuda_error("cudaFuncSetAttribute(stream_step_kernel)", e);
         configured = smem;
     }
-    stream_step_kernel<IPT><<<blocks, threads, smem, st>>>(a);
+    stream_step_kernel<IPT, MAXT><<<blocks, threads, smem, st>>>(a);
     return check_launch("stream_step_kernel");
+}
+
+// The narrowest instantiation of IPT items a thread that takes `threads`.
+template <int IPT>
+static int launch_fit(const StreamArgs &a, unsigned blocks, int threads, int smem, cudaStream_t st) {
+    if (threads <= stream_max_threads(IPT)) return launch_ipt<IPT>(a, blocks, threads, smem, st);
+    if constexpr (stream_max_threads(IPT) < kStreamWide1)
+        if (threads <= kStreamWide1) return launch_ipt<IPT, kStreamWide1>(a, blocks, threads, smem, st);
+    return launch_ipt<IPT, kStreamWide2>(a, blocks, threads, smem, st);
 }
 
 int stream_smem_bytes(int tj, int kp, int stages) {
@@ -525,13 +534,13 @@ int launch_stream_step(const pic_grid *g, const StreamShape &sh, const void *pos
     if (blocks > kMaxStepBlocks) blocks = kMaxStepBlocks;
     const int threads = (a.consumer_warps + 1) * 32;
     const int ipt = (a.tj * a.c4 + a.consumer_warps * 32 - 1) / (a.consumer_warps * 32);
-    if (ipt >= 1 && ipt <= kStreamMaxIpt && threads > stream_max_threads(ipt))
+    if (ipt >= 1 && ipt <= kStreamMaxIpt && threads > stream_thread_limit(ipt))
         return set_error(PIC_E_INVALID, "stream variant: too many consumer warps for this tile (registers)");
     switch (ipt) {
         case 1: return launch_ipt<1>(a, (unsigned)blocks, threads, smem, st);
-        case 2: return launch_ipt<2>(a, (unsigned)blocks, threads, smem, st);
-        case 3: return launch_ipt<3>(a, (unsigned)blocks, threads, smem, st);
-        case 4: return launch_ipt<4>(a, (unsigned)blocks, threads, smem, st);
+        case 2: return launch_fit<2>(a, (unsigned)blocks, threads, smem, st);
+        case 3: return launch_fit<3>(a, (unsigned)blocks, threads, smem, st);
+        case 4: return launch_fit<4>(a, (unsigned)blocks, threads, smem, st);
         case 5: return launch_ipt<5>(a, (unsigned)blocks, threads, smem, st);
         case 6: return launch_ipt<6>(a, (unsigned)blocks, threads, smem, st);
         default:

@@ -254,14 +254,27 @@ def test_multistep_float64_matches_the_oracle(oracle, wall):
                                atol=1e-10 * np.abs(ref["recombined"]).max())
 
 
+LARGE_STREAM_SHAPES = {
+    "default": {"variant": "stream"},
+    # 12 consumer warps, 4 and 3 k-vectors a thread: the kernel's wide forms
+    "wide4": {"variant": "stream", "tile_rows": 15, "consumer_warps": 12, "stages": 4},
+    "wide3": {"variant": "stream", "tile_rows": 11, "consumer_warps": 12, "stages": 5},
+    "wide3_15": {"variant": "stream", "tile_rows": 14, "consumer_warps": 15, "stages": 4},
+    # 16 consumer warps, 2 and 3 k-vectors a thread (17-warp forms)
+    "wide2_16": {"variant": "stream", "tile_rows": 10, "consumer_warps": 16, "stages": 5},
+    "wide3_16": {"variant": "stream", "tile_rows": 15, "consumer_warps": 16, "stages": 4},
+}
+
+
+@pytest.mark.parametrize("shape", sorted(LARGE_STREAM_SHAPES))
 @pytest.mark.parametrize("wall", ["absorbing", "reflecting"])
-def test_stream_and_flat_agree_on_a_large_grid(wall):
+def test_stream_and_flat_agree_on_a_large_grid(wall, shape):
     """208 x 208 x 406 (5 um, r = 0.05 cm), 40 steps of the pulse at 89.1 Gy/s
     (~3 000 tracks a step): the two kernels give the same fields and tallies
     to float32 rounding."""
     cfg = make_config("column_5um_r05_d89p1", lateral_boundary=wall)
     a = _solver()(cfg, progress=False, max_steps=40, shape={"variant": "flat"})
-    b = _solver()(cfg, progress=False, max_steps=40, shape={"variant": "stream"})
+    b = _solver()(cfg, progress=False, max_steps=40, shape=LARGE_STREAM_SHAPES[shape])
     np.testing.assert_array_equal(a.track_density_xy, b.track_density_xy)
     for x, y in [(a.recombination, b.recombination), (a.n_positive, b.n_positive), (a.injected_positive,
                                                                                      b.injected_positive)]:
