@@ -244,7 +244,10 @@ int pic_arrival_counts_pcg64(uint64_t *state, int64_t n, double duration, const 
  * descriptor's weights are lat = s, zm = s + c(c+1)/2, zp = s + c(c-1)/2,
  * cen = 1 - c^2 - 6s), at fixed dt. Reflecting wall: lam_*_in
  * is modified (the ring's adjoint is folded into the interior columns it
- * copies). Workspace: pic_adjoint_workspace_bytes, zeroed once.
+ * copies). lambda is zero on the z end planes (k = 0, nzb-1) and the row
+ * padding: lam_*_out is written so, and lam_*_in must be so (u there is fixed
+ * at zero; lambda_{n_steps} = 0 and every step keep it). Workspace:
+ * pic_adjoint_workspace_bytes, zeroed once.
  */
 int pic_adjoint_workspace_bytes(const pic_grid *g, int64_t *bytes);
 int pic_adjoint_step(const pic_grid *g, const void *pos, const void *neg, const void *dens, void *lam_pos_in,

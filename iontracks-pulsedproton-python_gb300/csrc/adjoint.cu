@@ -34,6 +34,11 @@
 // per-weight sums they combine are large and nearly equal, and subtracting
 // them after summation would cancel most of the float32 digits. The
 // deposition is a constant of every step: it enters only through u~.
+//
+// lambda_s is written as zero on the z end planes (k = 0, nzb-1) and the row
+// padding: u there is fixed at zero whatever the parameters, so its adjoint
+// never enters a derivative (the stencil reads mu there as zero). Every
+// adjoint step keeps the convention; lambda_{n_steps} = 0 starts it.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -181,16 +186,16 @@ __global__ void __launch_bounds__(BLOCK) adjoint_step_kernel(AdjArgs<T> a) {
                 lp += a.a * N.v[e];
                 ln += a.a * P.v[e];
             }
-            const bool pad = (k0 + e) >= a.nzb;
-            OP.v[e] = pad ? T(0) : lp;
-            ON.v[e] = pad ? T(0) : ln;
+            // zero on the end planes and the padding (see the header)
+            OP.v[e] = valid[e] ? lp : T(0);
+            ON.v[e] = valid[e] ? ln : T(0);
         }
         if (!interior && !a.reflecting) {  // absorbing ring: identity carry
             const V4<T> RP = load4(a.lp + off), RN = load4(a.ln + off);
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
-                OP.v[e] += (k0 + e) < a.nzb ? RP.v[e] : T(0);
-                ON.v[e] += (k0 + e) < a.nzb ? RN.v[e] : T(0);
+                OP.v[e] += valid[e] ? RP.v[e] : T(0);
+                ON.v[e] += valid[e] ? RN.v[e] : T(0);
             }
         }
         store4(a.lp_out + off, OP);

@@ -59,6 +59,13 @@ struct AdjStreamArgs {
 __device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
 __device__ __forceinline__ void st4(float *p, float4 v) { *reinterpret_cast<float4 *>(p) = v; }
 __device__ __forceinline__ float comp(const float4 &v, int e) { return (&v.x)[e]; }
+__device__ __forceinline__ float2 lo2(const float4 &v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(const float4 &v) { return make_float2(v.z, v.w); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
 
 int stage_floats(int tj, int kp) { return 4 * (tj + 2) * kp + 2 * ((tj + 8) & ~3); }
 
@@ -144,6 +151,13 @@ __global__ void __launch_bounds__((kAdjStreamWarps + 1) * 32, 1) adjoint_stream_
         // plane, slot s = row s / c4, k-vector s % c4
         const int ctid = threadIdx.x, nct = cw * 32;
         const int n = a.n, kp = a.kp, c4 = a.c4;
+        const float2 PZM = make_float2(a.p_zm, a.p_zm), PZP = make_float2(a.p_zp, a.p_zp);
+        const float2 PLT = make_float2(a.p_lat, a.p_lat), PCN = make_float2(a.p_cen, a.p_cen);
+        const float2 NZM = make_float2(a.n_zm, a.n_zm), NZP = make_float2(a.n_zp, a.n_zp);
+        const float2 NLT = make_float2(a.n_lat, a.n_lat), NCN = make_float2(a.n_cen, a.n_cen);
+        const float2 AD = make_float2(a.a, a.a), CPOS = make_float2(a.c_pos, a.c_pos);
+        const float2 CNEG = make_float2(a.c_neg, a.c_neg), HALF = make_float2(0.5f, 0.5f);
+        const float2 M2 = make_float2(-2.f, -2.f), M4 = make_float2(-4.f, -4.f);
         long long g = 0;
         for (int w = blockIdx.x; w < a.n_items; w += gridDim.x) {
             const int u = w / a.jt, t = w - u * a.jt;
@@ -167,6 +181,7 @@ __global__ void __launch_bounds__((kAdjStreamWarps + 1) * 32, 1) adjoint_stream_
                 const int dx = 2 * ci - a.two_mid;
                 const uint32_t dx2 = (uint32_t)(dx * dx);
                 const bool im_in = ci - 1 >= 1, ip_in = ci + 1 <= n - 2;  // i-neighbours interior
+                float2 G0 = make_float2(0.f, 0.f), G1 = G0, G2 = G0, G3 = G0, G4 = G0;
 #pragma unroll
                 for (int kk = 0; kk < IPT; ++kk) {
                     const int sl = ctid + kk * nct;
@@ -176,77 +191,77 @@ __global__ void __launch_bounds__((kAdjStreamWarps + 1) * 32, 1) adjoint_stream_
                     const int cj = cj_lo + r;
                     const int k0 = 4 * c;
                     const int o = rs * kp + k0;
-                    bool g4[4], valid[4];
+                    bool g4[4], valid[4], sc[4];
+                    const int dy = 2 * cj - a.two_mid;
+                    const bool scored = dx2 + (uint32_t)(dy * dy) <= a.thr4;
 #pragma unroll
                     for (int e = 0; e < 4; ++e) {
                         g4[e] = (k0 + e >= a.nze) && (k0 + e < a.gap_end);
                         valid[e] = (k0 + e >= 1) && (k0 + e <= a.nzb - 2);
+                        sc[e] = scored && g4[e];
                     }
-                    const int dy = 2 * cj - a.two_mid;
-                    const bool scored = dx2 + (uint32_t)(dy * dy) <= a.thr4;
                     const float2 dpr = has_dens ? reinterpret_cast<const float2 *>(Sc + dens_off)[dq + rs]
                                                 : make_float2(0.f, 0.f);
-                    const float dc = dpr.x, dl = dpr.y;
+                    const float dc = dpr.x, dl = dpr.y;  // this column's deposition, its neighbours' sum
                     const bool jm_in = cj - 1 >= 1, jp_in = cj + 1 <= n - 2;
 
-                    // mu = lambda_{s+1} on interior columns and valid k
-                    auto mu4 = [&](const float *p, bool in) {
-                        float4 m = in ? lds4(p) : make_float4(0.f, 0.f, 0.f, 0.f);
-                        m.x = valid[0] ? m.x : 0.f;
-                        m.y = valid[1] ? m.y : 0.f;
-                        m.z = valid[2] ? m.z : 0.f;
-                        m.w = valid[3] ? m.w : 0.f;
-                        return m;
-                    };
-                    const float4 MP = mu4(Sc + o, true), MN = mu4(Sc + spec + o, true);
-                    const bool km_ok = k0 - 1 >= 1, kp_ok = k0 + 4 <= a.nzb - 2;
-                    const float mp_km = km_ok ? Sc[o - 1] : 0.f, mp_kp = kp_ok ? Sc[o + 4] : 0.f;
-                    const float mn_km = km_ok ? Sc[spec + o - 1] : 0.f, mn_kp = kp_ok ? Sc[spec + o + 4] : 0.f;
-                    // lateral sums of mu, in the order i-1, i+1, j-1, j+1
-                    float4 LP, LN;
-                    {
-                        const float4 A0 = mu4(Sm + o, im_in), B0 = mu4(Sm + spec + o, im_in);
-                        const float4 A1 = mu4(Sp + o, ip_in), B1 = mu4(Sp + spec + o, ip_in);
-                        const float4 A2 = mu4(Sc + o - kp, jm_in), B2 = mu4(Sc + spec + o - kp, jm_in);
-                        const float4 A3 = mu4(Sc + o + kp, jp_in), B3 = mu4(Sc + spec + o + kp, jp_in);
-                        LP.x = ((0.f + A0.x) + A1.x + A2.x) + A3.x; LN.x = ((0.f + B0.x) + B1.x + B2.x) + B3.x;
-                        LP.y = ((0.f + A0.y) + A1.y + A2.y) + A3.y; LN.y = ((0.f + B0.y) + B1.y + B2.y) + B3.y;
-                        LP.z = ((0.f + A0.z) + A1.z + A2.z) + A3.z; LN.z = ((0.f + B0.z) + B1.z + B2.z) + B3.z;
-                        LP.w = ((0.f + A0.w) + A1.w + A2.w) + A3.w; LN.w = ((0.f + B0.w) + B1.w + B2.w) + B3.w;
-                    }
+                    // mu = lambda_{s+1}: zero on the end planes and the padding as
+                    // every adjoint step writes it; zero on ring columns by the
+                    // interior tests of the neighbours
+                    const float4 MP = lds4(Sc + o), MN = lds4(Sc + spec + o);
+                    const float mp_km = k0 >= 1 ? Sc[o - 1] : 0.f, mn_km = k0 >= 1 ? Sc[spec + o - 1] : 0.f;
+                    const float mp_kp = k0 + 4 < kp ? Sc[o + 4] : 0.f, mn_kp = k0 + 4 < kp ? Sc[spec + o + 4] : 0.f;
+                    const float4 Z = make_float4(0.f, 0.f, 0.f, 0.f);
+                    const float4 A0 = im_in ? lds4(Sm + o) : Z, B0 = im_in ? lds4(Sm + spec + o) : Z;
+                    const float4 A1 = ip_in ? lds4(Sp + o) : Z, B1 = ip_in ? lds4(Sp + spec + o) : Z;
+                    const float4 A2 = jm_in ? lds4(Sc + o - kp) : Z, B2 = jm_in ? lds4(Sc + spec + o - kp) : Z;
+                    const float4 A3 = jp_in ? lds4(Sc + o + kp) : Z, B3 = jp_in ? lds4(Sc + spec + o + kp) : Z;
+                    // lateral sums of mu in the order i-1, i+1, j-1, j+1
+                    const float2 LPl = add2(add2(add2(lo2(A0), lo2(A1)), lo2(A2)), lo2(A3));
+                    const float2 LPh = add2(add2(add2(hi2(A0), hi2(A1)), hi2(A2)), hi2(A3));
+                    const float2 LNl = add2(add2(add2(lo2(B0), lo2(B1)), lo2(B2)), lo2(B3));
+                    const float2 LNh = add2(add2(add2(hi2(B0), hi2(B1)), hi2(B2)), hi2(B3));
                     // centre state u~ (this step's deposition on gap layers)
-                    float4 P = lds4(Sc + 2 * spec + o), N = lds4(Sc + 3 * spec + o);
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) {
-                        (&P.x)[e] += g4[e] ? dc : 0.f;
-                        (&N.x)[e] += g4[e] ? dc : 0.f;
-                    }
-                    float4 OP, ON;
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) {
-                        const float mp = comp(MP, e), mn = comp(MN, e);
-                        const float mp_up = e < 3 ? comp(MP, e + 1) : mp_kp, mp_dn = e > 0 ? comp(MP, e - 1) : mp_km;
-                        const float mn_up = e < 3 ? comp(MN, e + 1) : mn_kp, mn_dn = e > 0 ? comp(MN, e - 1) : mn_km;
-                        const float msum = mp + mn;
-                        const bool sc = scored && g4[e];
-                        float lp = a.p_zm * mp_up + a.p_zp * mp_dn + a.p_lat * comp(LP, e) + a.p_cen * mp -
-                                   a.a * comp(N, e) * msum;
-                        float ln = a.n_zm * mn_dn + a.n_zp * mn_up + a.n_lat * comp(LN, e) + a.n_cen * mn -
-                                   a.a * comp(P, e) * msum;
-                        if (sc) {
-                            lp += a.a * comp(N, e);
-                            ln += a.a * comp(P, e);
-                        }
-                        const bool pad = (k0 + e) >= a.nzb;
-                        (&OP.x)[e] = pad ? 0.f : lp;
-                        (&ON.x)[e] = pad ? 0.f : ln;
-                    }
+                    const float2 DCl = make_float2(g4[0] ? dc : 0.f, g4[1] ? dc : 0.f);
+                    const float2 DCh = make_float2(g4[2] ? dc : 0.f, g4[3] ? dc : 0.f);
+                    const float4 P0 = lds4(Sc + 2 * spec + o), N0 = lds4(Sc + 3 * spec + o);
+                    const float2 Pl = add2(lo2(P0), DCl), Ph = add2(hi2(P0), DCh);
+                    const float2 Nl = add2(lo2(N0), DCl), Nh = add2(hi2(N0), DCh);
+                    const float2 MPl = lo2(MP), MPh = hi2(MP), MNl = lo2(MN), MNh = hi2(MN);
+                    // k+1 / k-1 neighbours of the four elements
+                    const float2 mpu_l = make_float2(MP.y, MP.z), mpu_h = make_float2(MP.w, mp_kp);
+                    const float2 mpd_l = make_float2(mp_km, MP.x), mpd_h = make_float2(MP.y, MP.z);
+                    const float2 mnu_l = make_float2(MN.y, MN.z), mnu_h = make_float2(MN.w, mn_kp);
+                    const float2 mnd_l = make_float2(mn_km, MN.x), mnd_h = make_float2(MN.y, MN.z);
+                    const float2 Ssl = add2(MPl, MNl), Ssh = add2(MPh, MNh);  // mu+ + mu-
+                    const float2 ANl = mul2(AD, Nl), ANh = mul2(AD, Nh), APl = mul2(AD, Pl), APh = mul2(AD, Ph);
+                    // lambda+ = zm mu+[k+1] + zp mu+[k-1] + lat L+ + cen mu+ - a n~ (mu+ + mu-)
+                    // lambda- = zm mu-[k-1] + zp mu-[k+1] + lat L- + cen mu- - a p~ (mu+ + mu-)
+                    float2 lpl = fma2(PCN, MPl, fma2(PLT, LPl, fma2(PZP, mpd_l, mul2(PZM, mpu_l))));
+                    float2 lph = fma2(PCN, MPh, fma2(PLT, LPh, fma2(PZP, mpd_h, mul2(PZM, mpu_h))));
+                    float2 lnl = fma2(NCN, MNl, fma2(NLT, LNl, fma2(NZP, mnu_l, mul2(NZM, mnd_l))));
+                    float2 lnh = fma2(NCN, MNh, fma2(NLT, LNh, fma2(NZP, mnu_h, mul2(NZM, mnd_h))));
+                    lpl = fma2(neg2(ANl), Ssl, lpl);
+                    lph = fma2(neg2(ANh), Ssh, lph);
+                    lnl = fma2(neg2(APl), Ssl, lnl);
+                    lnh = fma2(neg2(APh), Ssh, lnh);
+                    // scored gap voxels: + a n~ (positive), + a p~ (negative)
+                    lpl = add2(lpl, make_float2(sc[0] ? ANl.x : 0.f, sc[1] ? ANl.y : 0.f));
+                    lph = add2(lph, make_float2(sc[2] ? ANh.x : 0.f, sc[3] ? ANh.y : 0.f));
+                    lnl = add2(lnl, make_float2(sc[0] ? APl.x : 0.f, sc[1] ? APl.y : 0.f));
+                    lnh = add2(lnh, make_float2(sc[2] ? APh.x : 0.f, sc[3] ? APh.y : 0.f));
+                    // zero on the end planes and the padding
+                    const float4 OP = make_float4(valid[0] ? lpl.x : 0.f, valid[1] ? lpl.y : 0.f,
+                                                  valid[2] ? lph.x : 0.f, valid[3] ? lph.y : 0.f);
+                    const float4 ON = make_float4(valid[0] ? lnl.x : 0.f, valid[1] ? lnl.y : 0.f,
+                                                  valid[2] ? lnh.x : 0.f, valid[3] ? lnh.y : 0.f);
                     const int64_t col = (int64_t)ci * n + cj;
                     st4(a.lp_out + col * kp + k0, OP);
                     st4(a.ln_out + col * kp + k0, ON);
 
                     // ring columns next to this interior column: (ri, cj),
                     // (ci, rj) get lat * mu + carry; the corner (ri, rj) the carry
+                    // (mu and the carry are zero on the end planes and padding)
                     const bool lo_i = ci == 1, hi_i = ci == n - 2, lo_j = cj == 1, hi_j = cj == n - 2;
                     if (lo_i || hi_i || lo_j || hi_j) {
                         for (int tgt = 0; tgt < 3; ++tgt) {
@@ -278,16 +293,8 @@ __global__ void __launch_bounds__((kAdjStreamWarps + 1) * 32, 1) adjoint_stream_
                                 const float4 CP = lds4(Sr + row * kp + k0), CN = lds4(Sr + spec + row * kp + k0);
 #pragma unroll
                                 for (int e = 0; e < 4; ++e) {
-                                    const bool in_k = (k0 + e) < a.nzb;
-                                    (&RP.x)[e] = (in_k ? (&RP.x)[e] : 0.f) + (in_k ? comp(CP, e) : 0.f);
-                                    (&RN.x)[e] = (in_k ? (&RN.x)[e] : 0.f) + (in_k ? comp(CN, e) : 0.f);
-                                }
-                            } else {
-#pragma unroll
-                                for (int e = 0; e < 4; ++e) {
-                                    const bool pad = (k0 + e) >= a.nzb;
-                                    (&RP.x)[e] = pad ? 0.f : (&RP.x)[e];
-                                    (&RN.x)[e] = pad ? 0.f : (&RN.x)[e];
+                                    (&RP.x)[e] += comp(CP, e);
+                                    (&RN.x)[e] += comp(CN, e);
                                 }
                             }
                             const int64_t rcol = (int64_t)ri * n + rj;
@@ -296,46 +303,52 @@ __global__ void __launch_bounds__((kAdjStreamWarps + 1) * 32, 1) adjoint_stream_
                         }
                     }
 
-                    // derivative sums of this column's outputs
-                    const float pkm = k0 >= 1 ? Sc[2 * spec + o - 1] + ((k0 - 1 >= a.nze && k0 - 1 < a.gap_end) ? dc : 0.f) : 0.f;
-                    const float nkm = k0 >= 1 ? Sc[3 * spec + o - 1] + ((k0 - 1 >= a.nze && k0 - 1 < a.gap_end) ? dc : 0.f) : 0.f;
-                    const float pkp = k0 + 4 < kp ? Sc[2 * spec + o + 4] + ((k0 + 4 >= a.nze && k0 + 4 < a.gap_end) ? dc : 0.f) : 0.f;
-                    const float nkp = k0 + 4 < kp ? Sc[3 * spec + o + 4] + ((k0 + 4 >= a.nze && k0 + 4 < a.gap_end) ? dc : 0.f) : 0.f;
-                    float4 SP, SN;
-                    {
-                        const float4 A0 = lds4(Sm + 2 * spec + o), B0 = lds4(Sm + 3 * spec + o);
-                        const float4 A1 = lds4(Sp + 2 * spec + o), B1 = lds4(Sp + 3 * spec + o);
-                        const float4 A2 = lds4(Sc + 2 * spec + o - kp), B2 = lds4(Sc + 3 * spec + o - kp);
-                        const float4 A3 = lds4(Sc + 2 * spec + o + kp), B3 = lds4(Sc + 3 * spec + o + kp);
-#pragma unroll
-                        for (int e = 0; e < 4; ++e) {
-                            (&SP.x)[e] = (((0.f + comp(A0, e)) + comp(A1, e)) + comp(A2, e)) + comp(A3, e);
-                            (&SN.x)[e] = (((0.f + comp(B0, e)) + comp(B1, e)) + comp(B2, e)) + comp(B3, e);
-                            (&SP.x)[e] += g4[e] ? dl : 0.f;
-                            (&SN.x)[e] += g4[e] ? dl : 0.f;
-                        }
-                    }
-                    float gs[kAdjGrad] = {0.f, 0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) {
-                        const float mp = comp(MP, e), mn = comp(MN, e);
-                        const float p = comp(P, e), nn = comp(N, e);
-                        const float p_dn = e > 0 ? comp(P, e - 1) : pkm, p_up = e < 3 ? comp(P, e + 1) : pkp;
-                        const float n_dn = e > 0 ? comp(N, e - 1) : nkm, n_up = e < 3 ? comp(N, e + 1) : nkp;
-                        const float pz2 = (p_dn + p_up) - 2.f * p, nz2 = (n_dn + n_up) - 2.f * nn;
-                        const float plap = (comp(SP, e) - 4.f * p) + pz2, nlap = (comp(SN, e) - 4.f * nn) + nz2;
-                        const float pc = 0.5f * (p_dn - p_up) + a.c_pos * pz2;
-                        const float nc = 0.5f * (n_up - n_dn) + a.c_neg * nz2;
-                        const float pn = p * nn;
-                        gs[0] += mp * plap;
-                        gs[1] += mp * pc;
-                        gs[2] += mn * nlap;
-                        gs[3] += mn * nc;
-                        gs[4] += ((scored && g4[e]) ? pn : 0.f) - (mp + mn) * pn;
-                    }
-#pragma unroll
-                    for (int qq = 0; qq < kAdjGrad; ++qq) acc[qq].add(gs[qq]);
+                    // derivative sums of this column's outputs (mu is zero where
+                    // k is not valid, so no masks)
+                    const float dkm = (k0 - 1 >= a.nze && k0 - 1 < a.gap_end) ? dc : 0.f;
+                    const float dkp = (k0 + 4 >= a.nze && k0 + 4 < a.gap_end) ? dc : 0.f;
+                    const float pkm = k0 >= 1 ? Sc[2 * spec + o - 1] + dkm : 0.f;
+                    const float nkm = k0 >= 1 ? Sc[3 * spec + o - 1] + dkm : 0.f;
+                    const float pkp = k0 + 4 < kp ? Sc[2 * spec + o + 4] + dkp : 0.f;
+                    const float nkp = k0 + 4 < kp ? Sc[3 * spec + o + 4] + dkp : 0.f;
+                    const float4 S0 = lds4(Sm + 2 * spec + o), T0 = lds4(Sm + 3 * spec + o);
+                    const float4 S1 = lds4(Sp + 2 * spec + o), T1 = lds4(Sp + 3 * spec + o);
+                    const float4 S2 = lds4(Sc + 2 * spec + o - kp), T2 = lds4(Sc + 3 * spec + o - kp);
+                    const float4 S3 = lds4(Sc + 2 * spec + o + kp), T3 = lds4(Sc + 3 * spec + o + kp);
+                    const float2 DLl = make_float2(g4[0] ? dl : 0.f, g4[1] ? dl : 0.f);
+                    const float2 DLh = make_float2(g4[2] ? dl : 0.f, g4[3] ? dl : 0.f);
+                    const float2 SPl = add2(add2(add2(add2(lo2(S0), lo2(S1)), lo2(S2)), lo2(S3)), DLl);
+                    const float2 SPh = add2(add2(add2(add2(hi2(S0), hi2(S1)), hi2(S2)), hi2(S3)), DLh);
+                    const float2 SNl = add2(add2(add2(add2(lo2(T0), lo2(T1)), lo2(T2)), lo2(T3)), DLl);
+                    const float2 SNh = add2(add2(add2(add2(hi2(T0), hi2(T1)), hi2(T2)), hi2(T3)), DLh);
+                    const float2 pdl = make_float2(pkm, Pl.x), pdh = make_float2(Pl.y, Ph.x);
+                    const float2 pul = make_float2(Pl.y, Ph.x), puh = make_float2(Ph.y, pkp);
+                    const float2 ndl = make_float2(nkm, Nl.x), ndh = make_float2(Nl.y, Nh.x);
+                    const float2 nul = make_float2(Nl.y, Nh.x), nuh = make_float2(Nh.y, nkp);
+                    // z second difference, 7-point Laplacian, Courant derivative
+                    const float2 pz2l = fma2(M2, Pl, add2(pdl, pul)), pz2h = fma2(M2, Ph, add2(pdh, puh));
+                    const float2 nz2l = fma2(M2, Nl, add2(ndl, nul)), nz2h = fma2(M2, Nh, add2(ndh, nuh));
+                    const float2 plapl = add2(fma2(M4, Pl, SPl), pz2l), plaph = add2(fma2(M4, Ph, SPh), pz2h);
+                    const float2 nlapl = add2(fma2(M4, Nl, SNl), nz2l), nlaph = add2(fma2(M4, Nh, SNh), nz2h);
+                    const float2 pcl = fma2(CPOS, pz2l, mul2(HALF, sub2(pdl, pul)));
+                    const float2 pch = fma2(CPOS, pz2h, mul2(HALF, sub2(pdh, puh)));
+                    const float2 ncl = fma2(CNEG, nz2l, mul2(HALF, sub2(nul, ndl)));
+                    const float2 nch = fma2(CNEG, nz2h, mul2(HALF, sub2(nuh, ndh)));
+                    const float2 pnl = mul2(Pl, Nl), pnh = mul2(Ph, Nh);
+                    G0 = fma2(MPh, plaph, fma2(MPl, plapl, G0));
+                    G1 = fma2(MPh, pch, fma2(MPl, pcl, G1));
+                    G2 = fma2(MNh, nlaph, fma2(MNl, nlapl, G2));
+                    G3 = fma2(MNh, nch, fma2(MNl, ncl, G3));
+                    G4 = fma2(neg2(Ssh), pnh, fma2(neg2(Ssl), pnl, G4));
+                    G4 = add2(G4, make_float2(sc[0] ? pnl.x : 0.f, sc[1] ? pnl.y : 0.f));
+                    G4 = add2(G4, make_float2(sc[2] ? pnh.x : 0.f, sc[3] ? pnh.y : 0.f));
                 }
+                // this plane's sums of the thread's items, into the compensated totals
+                acc[0].add(G0.x + G0.y);
+                acc[1].add(G1.x + G1.y);
+                acc[2].add(G2.x + G2.y);
+                acc[3].add(G3.x + G3.y);
+                acc[4].add(G4.x + G4.y);
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&empty[sm_]);
                 sm_ = sc_; pm_ = pc_;
