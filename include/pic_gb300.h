@@ -84,7 +84,7 @@ typedef struct pic_grid {
  * through L1/L2, any grid and either field type. STREAM: float32 only; whole
  * (j-tile x k-row) planes staged in shared memory by bulk asynchronous copies
  * while the CTA marches along i, for grids with no_xy >= 16. AUTO picks
- * STREAM for float32 grids with no_xy >= 64 and no_xy^2 * kpitch >= 2e8 cells,
+ * STREAM for float32 grids with no_xy >= 64 and no_xy^2 * kpitch >= 1e8 cells,
  * FLAT otherwise; planes_per_item 0 gives about 12 work items per SM,
  * consumer_warps 0 gives 13, tile_rows 0 about three k-vectors a consumer
  * thread, stages 0 as many as shared memory holds. */

@@ -79,9 +79,10 @@ int score_test(const pic_grid *g, ScoreTest *out) {
 int resolve_shape(pic_grid *g) {
     // Measured on GB300 (graph-replayed steps, idle / pulse): the flat kernel
     // is faster up to a few hundred lateral cells (62.6 / 77.9 us vs 86.4 /
-    // 95.8 us at 208x208x408; 146 / 174 vs 176 / 191 us at 328x328x408),
-    // even at 608x608x408 (476 / 573 vs 518 / 563 us); the streaming kernel
-    // wins at the 1068x1068x408 full electrode (1.58 / 1.71 vs 1.73 / 1.95 ms).
+    // 95.8 us at 208x208x408; 146 / 174 vs 176 / 191 us at 328x328x408); the
+    // streaming kernel in its 13-consumer-warp form wins from 608x608x408
+    // (437 / 438 vs 454 / 492 us) to the 1068x1068x408 full electrode (1.250 /
+    // 1.255 ms vs 1.73 / 1.95 ms).
     if (g->variant == PIC_VARIANT_AUTO)
         g->variant = (g->dtype == PIC_F32 && g->no_xy >= 64 && g->no_xy * g->no_xy * g->kpitch >= kStreamMinCells)
                          ? PIC_VARIANT_STREAM

@@ -78,7 +78,7 @@ __host__ __device__ inline int deposit_parts(int64_t m, int sms) {
 }
 
 // AUTO picks the streaming kernel from this many allocated cells (no_xy^2 * kpitch)
-constexpr int64_t kStreamMinCells = 200000000;
+constexpr int64_t kStreamMinCells = 100000000;
 
 // Launch shape of the streaming step kernel.
 struct StreamShape {

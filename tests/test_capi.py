@@ -128,7 +128,7 @@ def test_launch_shape_resolution_without_a_gpu():
     assert 32 <= s["planes_per_item"] <= 64
     small = eng.make_grid(make_config("column_10um_r008"))
     assert eng.resolve_shape(small)["variant"] == "flat"
-    # 208 x 208 x 408 = 17.7 M cells: flat by default (faster below ~2e8
+    # 208 x 208 x 408 = 17.7 M cells: flat by default (faster below ~1e8
     # cells); streaming when asked, with few planes per item so that 30
     # j-tiles still give every SM work
     mid = eng.make_grid(make_config("column_5um_r05_d8p91"))
