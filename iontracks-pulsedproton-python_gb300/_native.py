@@ -23,6 +23,8 @@ PIC_WALL_REFLECTING = 1
 PIC_VARIANT_AUTO = 0
 PIC_VARIANT_FLAT = 1
 PIC_VARIANT_STREAM = 2
+# pic_abi_version() of the library these structures mirror
+ABI_VERSION = 4
 
 _LIB_PATH = Path(__file__).resolve().parent / "_build" / "libpic_gb300.so"
 _lock = threading.Lock()
@@ -214,6 +216,10 @@ def load(path: Path | None = None, build_if_missing: bool = True):
             fn = getattr(L, name)
             fn.restype = res
             fn.argtypes = args
+        # a library built from other sources would read these structures wrong
+        if L.pic_abi_version() != ABI_VERSION:
+            raise RuntimeError(f"{p} has ABI {L.pic_abi_version()}, this binding ABI {ABI_VERSION}: rebuild it "
+                               "with the package's build.py")
         if path is None:
             _lib = L
         return L

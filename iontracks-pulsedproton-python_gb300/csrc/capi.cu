@@ -263,6 +263,10 @@ extern "C" {
 
 const char *pic_last_error(void) { return g_last_error.c_str(); }
 
+// The Python binding mirrors pic_grid field by field (ABI 4: 5 int64, 14
+// double, 9 int32, padded to 8 bytes).
+static_assert(sizeof(pic_grid) == 192, "pic_grid layout changed: bump pic_abi_version and the bindings");
+
 int pic_abi_version(void) { return 4; }
 
 int64_t pic_kpitch(int64_t nzb) { return (nzb + 7) / 8 * 8; }
