@@ -187,8 +187,8 @@ __global__ void __launch_bounds__(MAXT, 1) stream_step_kernel(StreamArgs a) {
         // masked one. Work slot s of a plane is core item s (row s / ncore,
         // vector c_lo + s % ncore) for s < n_core, then edge items; consumer
         // thread t owns slots t + k * nct, k < IPT, so consecutive lanes hold
-        // consecutive core vectors of a row and trade their edge elements (the
-        // k-1 / k+4 neighbours) by shuffle.
+        // consecutive core vectors of a row (their k-1 / k+4 neighbours are
+        // read from shared memory).
         const int ctid = threadIdx.x;
         const int nct = cw * 32;
         const int n = a.n, kp = a.kp, c4 = a.c4;
@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(MAXT, 1) stream_step_kernel(StreamArgs a) {
                     const int kd = kind[k], rs = rs_[k], c = c_[k];
                     const int k0 = 4 * c;
                     const int o = rs * kp + k0;
-                    // convergent part: centre vectors, densities, edge shuffles
+                    // centre vectors and this column's densities
                     float4 P = lds4(Sc + o), N = lds4(Sc + spec + o);
                     const float2 dpair = has_dens ? reinterpret_cast<const float2 *>(Sc + dens_off)[dq + rs]
                                                   : make_float2(0.f, 0.f);
@@ -272,28 +272,25 @@ __global__ void __launch_bounds__(MAXT, 1) stream_step_kernel(StreamArgs a) {
                         P.x += dcen; P.y += dcen; P.z += dcen; P.w += dcen;
                         N.x += dcen; N.y += dcen; N.z += dcen; N.w += dcen;
                     }
-                    const float up_p = __shfl_up_sync(0xffffffffu, P.w, 1);
-                    const float up_n = __shfl_up_sync(0xffffffffu, N.w, 1);
-                    const float dn_p = __shfl_down_sync(0xffffffffu, P.x, 1);
-                    const float dn_n = __shfl_down_sync(0xffffffffu, N.x, 1);
                     if (kd == 0) continue;
                     const int cj = cj_lo + rs - 1;
                     const bool scored = (dx2 + dy2[k] <= a.thr4);
                     float4 PO, NO;
                     if (kd == 1) {
                         // ---- core vector: mask-free, packed FP32x2 ----
-                        // neighbour lane's vector when it holds the adjacent vector
-                        // of the same row, else shared memory (+ its deposition)
-                        float pkm = up_p, nkm = up_n, pkp = dn_p, nkp = dn_n;
-                        if (lane == 0 || c == c_lo) {
-                            const float d = (c > c_lo || gap_below) ? dcen : 0.f;
-                            pkm = Sc[o - 1] + d;
-                            nkm = Sc[spec + o - 1] + d;
-                        }
-                        if (lane == 31 || c == c_hi - 1) {
-                            const float d = (c < c_hi - 1 || gap_above) ? dcen : 0.f;
-                            pkp = Sc[o + 4] + d;
-                            nkp = Sc[spec + o + 4] + d;
+                        // k-1 / k+4 neighbours from shared memory (+ their
+                        // deposition when they lie in the gap): uniform across the
+                        // warp, where shuffles needed a divergent fallback at the
+                        // warp's and the core's ends (measured 1.255 -> 1.201 ms a
+                        // full-electrode step)
+                        float pkm, nkm, pkp, nkp;
+                        {
+                            const float dm = (c > c_lo || gap_below) ? dcen : 0.f;
+                            const float dp = (c < c_hi - 1 || gap_above) ? dcen : 0.f;
+                            pkm = Sc[o - 1] + dm;
+                            nkm = Sc[spec + o - 1] + dm;
+                            pkp = Sc[o + 4] + dp;
+                            nkp = Sc[spec + o + 4] + dp;
                         }
                         const float4 Pjm = lds4(Sc + o - kp), Pjp = lds4(Sc + o + kp);
                         const float4 Pim = lds4(Sm + o), Pip = lds4(Sp + o);
