@@ -94,8 +94,8 @@ int resolve_shape(pic_grid *g) {
     const int kp = (int)g->kpitch, c4 = kp / 4;
     // default: 13 consumer warps (one 512-thread form, 128 registers a
     // thread) and tiles of about three k-vectors a thread -- on the full
-    // electrode 12 rows x 5 stages, within 2 % of the fastest of 2 150 shapes
-    // timed by the full autotuner (1.253 ms a step)
+    // electrode 12 rows x 5 stages, 1.216 ms a step, within 1.1 % of the
+    // fastest of 2 150 shapes timed by the full autotuner (15 warps, 1.202 ms)
     if (g->consumer_warps <= 0) g->consumer_warps = 13;
     if (g->consumer_warps > kStreamMaxThreads / 32 - 1)
         return set_error(PIC_E_INVALID, "consumer_warps must be <= " + std::to_string(kStreamMaxThreads / 32 - 1));
