@@ -32,11 +32,12 @@ from .feeder import TrackFeeder
 from .pulses import TrackSampler, build_track_schedule
 from .state import Diagnostics, collection_efficiency
 
-# The batched step runs 3 resident 256-thread blocks per SM (80 registers).
+# The batched step runs 4 resident 256-thread blocks per SM (float32, 64
+# registers).
 # Items per block are chosen per phase for about four blocks per resident slot:
 # few, long blocks amortise each block's set-up and reduction on the big
 # phases; enough blocks keep every SM busy when few small grids remain.
-BLOCKS_PER_SM = 3
+BLOCKS_PER_SM = 4
 WAVES = 4
 MIN_ITEMS_PER_BLOCK = 256
 MAX_ITEMS_PER_BLOCK = 1 << 16

@@ -177,8 +177,11 @@ __device__ __forceinline__ void batched_step_block(const BatchStepArgs<T> &b, in
     }
 }
 
+// float32: four resident blocks per SM (64 registers, a little spilled to
+// local memory) hide more of the heavy phase's global-load latency than three
+// at 80 registers (the 64-grid sweep: 1.12 against 1.15-1.19 s)
 template <typename T, int BLOCK, typename I>
-__global__ void __launch_bounds__(BLOCK) batched_step_kernel(BatchStepArgs<T> b) {
+__global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 4 : 1) batched_step_kernel(BatchStepArgs<T> b) {
     __shared__ typename RedT<T>::type red[BLOCK / 32][4];
     __shared__ bool last;
     // the block's grid arguments, staged once in shared memory and read by
