@@ -294,20 +294,26 @@ def run_batched_b200(
         N.check(lib.pic_step_workspace_bytes(ctypes.byref(grids[0]), ctypes.byref(swb)), "pic_step_workspace_bytes")
         solo_ws = torch.zeros(int(swb.value), dtype=torch.uint8, device=dev)
 
+    solo_graphs = []  # graph handles, freed once the run has finished
+
     def run_solo(c, c0, c1):
         """Grid c's global steps [c0, c1) with the single-grid kernels, on its
         slices: state of step s in buffer s & 1, deposition pairs in buffer
         s & 1 (the batched step clears the other one every step, as
-        pic_run_segment expects), tallies at row tally_off + s."""
+        pic_run_segment expects), tallies at row tally_off + s. The chunk's
+        launches are captured into one CUDA graph and replayed (small grids
+        are launch-bound)."""
         fo, do2 = field_off[c] * es, 2 * dens_off[c] * es
         off = np.ascontiguousarray(offsets[c][c0 : c1 + 1])
-        N.check(lib.pic_run_segment(
-            ctypes.byref(grids[c]), pos[0].data_ptr() + fo, neg[0].data_ptr() + fo, pos[1].data_ptr() + fo,
-            neg[1].data_ptr() + fo, c0 & 1, c1 - c0, xs_dev.data_ptr() + 8 * track_base[c],
-            ys_dev.data_ptr() + 8 * track_base[c], off.ctypes.data, dens[0].data_ptr() + do2,
-            dens[1].data_ptr() + do2, c0 & 1, counts.data_ptr() + 4 * counts_off[c],
-            tally.data_ptr() + 32 * (tally_off[c] + c0), solo_ws.data_ptr(), solo_ws.numel(), st),
-            "pic_run_segment")
+        args = (ctypes.byref(grids[c]), pos[0].data_ptr() + fo, neg[0].data_ptr() + fo, pos[1].data_ptr() + fo,
+                neg[1].data_ptr() + fo, c0 & 1, c1 - c0, xs_dev.data_ptr() + 8 * track_base[c],
+                ys_dev.data_ptr() + 8 * track_base[c], off.ctypes.data, dens[0].data_ptr() + do2,
+                dens[1].data_ptr() + do2, c0 & 1, counts.data_ptr() + 4 * counts_off[c],
+                tally.data_ptr() + 32 * (tally_off[c] + c0), solo_ws.data_ptr(), solo_ws.numel(), st)
+        h = ctypes.c_void_p()
+        N.check(lib.pic_graph_create(*args, ctypes.byref(h)), "pic_graph_create")
+        solo_graphs.append(h.value)
+        N.check(lib.pic_graph_launch(h.value, st), "pic_graph_launch")
 
     sto_dev = torch.from_numpy(step_task_off).to(dev)
     stt_dev = torch.from_numpy(np.ascontiguousarray(step_tracks, dtype=np.int64)).to(dev)
@@ -367,6 +373,9 @@ def run_batched_b200(
             if progress:
                 print(f"  global step {c1}/{S}")
         torch.cuda.synchronize(dev)
+        for h in solo_graphs:
+            lib.pic_graph_destroy(h)
+        solo_graphs.clear()
         if solo_ws is not None:
             sv = ctypes.c_int32()
             N.check(lib.pic_workspace_status(solo_ws.data_ptr(), 1, st, ctypes.byref(sv)), "pic_workspace_status")
@@ -381,6 +390,12 @@ def run_batched_b200(
                                    "results are invalid")
     finally:
         feeder.close()
+        if solo_graphs:  # an exception left graphs behind: let them finish, then free them
+            try:
+                torch.cuda.synchronize(dev)
+            finally:
+                for h in solo_graphs:
+                    lib.pic_graph_destroy(h)
     elapsed = perf_counter() - t0
 
     # --- one Result per configuration
