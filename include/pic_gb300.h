@@ -334,6 +334,17 @@ int pic_revolve_backward(const pic_grid *g, void *slots_pos, void *slots_neg, in
                          uintptr_t stream);
 
 /*
+ * pic_selftest_waits -- no counterpart in the reference: runs the kernels'
+ * two bounded waits against partners that never come, with short limits --
+ * the device-wide barrier of the persistent and multi-step kernels with one
+ * block that never arrives, and an mbarrier of the streaming kernels that
+ * nothing arrives on -- and returns the status codes they leave (5 for the
+ * barrier, 91 for the mbarrier: an expired wait). Neither faults or hangs;
+ * the context stays usable.
+ */
+int pic_selftest_waits(int32_t *barrier_status, int32_t *mbarrier_status, uintptr_t stream);
+
+/*
  * pic_capture_begin / pic_capture_end -- record every launch the library
  * issues on `stream` between the two calls (made from this host thread) into
  * a CUDA graph, instantiated and returned in *graph_out (replay with

@@ -133,6 +133,9 @@ EXPORTS = {
          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
          ctypes.c_int64, ctypes.c_void_p],
     ),
+    "pic_selftest_waits": (
+        ctypes.c_int, [ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p]
+    ),
     "pic_revolve_plan": (
         ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
     ),

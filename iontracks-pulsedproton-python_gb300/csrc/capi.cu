@@ -541,6 +541,11 @@ int pic_adjoint_backward(const pic_grid *g, const void *ckpt_pos, const void *ck
     return adjoint_accumulate_end(g, adj_workspace, grad, st);
 }
 
+int pic_selftest_waits(int32_t *barrier_status, int32_t *mbarrier_status, uintptr_t stream) {
+    if (!barrier_status || !mbarrier_status) return set_error(PIC_E_INVALID, "null pointer argument");
+    return selftest_waits(barrier_status, mbarrier_status, reinterpret_cast<cudaStream_t>(stream));
+}
+
 int pic_revolve_plan(int64_t n_steps, int64_t n_slots, int64_t *recompute_steps, int64_t *spine_levels) {
     return revolve_plan(n_steps, n_slots, recompute_steps, spine_levels);
 }

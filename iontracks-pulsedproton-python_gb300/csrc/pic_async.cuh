@@ -57,8 +57,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 
 // Waits until the phase with the given parity has completed. Returns false
 // (and stores `code` into *status) if the bound is reached.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *status, int code) {
-    for (long long it = 0; it < kWaitLimit; ++it)
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *status, int code,
+                                          long long limit = kWaitLimit) {
+    for (long long it = 0; it < limit; ++it)
         if (mbar_try_wait(bar, parity)) return true;
     if (status) atomicExch(status, code);
     return false;

@@ -22,7 +22,7 @@ struct BarrierRef {
     int *status;          // 0, or the code of a wait that gave up
 };
 
-__device__ __forceinline__ bool grid_barrier(BarrierRef bar) {
+__device__ __forceinline__ bool grid_barrier(BarrierRef bar, long long limit = kBarrierPolls) {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -42,7 +42,7 @@ __device__ __forceinline__ bool grid_barrier(BarrierRef bar) {
                     ok = 0;
                     break;
                 }
-                if (++polls > kBarrierPolls) {
+                if (++polls > limit) {
                     atomicCAS(bar.status, 0, kBarrierTimeout);
                     ok = 0;
                     break;

@@ -175,6 +175,8 @@ int revolve_backward(const pic_grid *g, void *slots_pos, void *slots_neg, int64_
                      void *lam_neg0, void *lam_pos1, void *lam_neg1, double *grad, void *ws, void *adj_ws,
                      cudaStream_t st);
 
+int selftest_waits(int32_t *barrier_status, int32_t *mbarrier_status, cudaStream_t st);
+
 int sample_disc(const double *u, int64_t n_pairs, double scale, double mid, double radius_sq, int64_t n_wanted,
                 double *xs, double *ys, int64_t *n_accepted, int64_t *n_pairs_used);
 int arrival_counts_pcg64(uint64_t *st, int64_t n, double duration, const double *edges, int64_t n_edges,

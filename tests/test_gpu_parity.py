@@ -11,6 +11,7 @@ Tolerances, per the project's parity bar:
   multiply-adds).
 """
 
+import ctypes
 import importlib
 import os
 
@@ -412,5 +413,24 @@ def test_autotuner_chooses_steps_per_launch():
     assert tried[chosen] == min(tried.values())
     eng.close()
     res = _solver()(cfg, progress=False, shape=best["shape"])
+    _check_f32(res, float(fx["ks"]), fx["injected"], fx["recombination"], fx["n_positive"], fx["n_negative"],
+               fx["track_density_xy"])
+
+
+def test_bounded_waits_expire_with_a_status_and_leave_the_context_usable():
+    """The kernels' two bounded waits, against partners that never come (a
+    device-wide barrier one block never reaches; an mbarrier nothing arrives
+    on), give up with their status codes instead of hanging; a run on the same
+    context afterwards still matches the reference."""
+    import torch
+
+    N = importlib.import_module(pkg().__name__ + "._native")
+    lib = N.load()
+    b, m = ctypes.c_int32(-1), ctypes.c_int32(-1)
+    N.check(lib.pic_selftest_waits(ctypes.byref(b), ctypes.byref(m), torch.cuda.current_stream().cuda_stream),
+            "pic_selftest_waits")
+    assert (b.value, m.value) == (5, 91)
+    cfg, fx = run_config("run_fast_base")
+    res = _solver()(cfg, progress=False)
     _check_f32(res, float(fx["ks"]), fx["injected"], fx["recombination"], fx["n_positive"], fx["n_negative"],
                fx["track_density_xy"])
