@@ -35,7 +35,7 @@ namespace pic {
 namespace {
 
 constexpr int kAdjStreamStages = 4;
-constexpr int kAdjStreamWarps = 12;  // consumer warps (full electrode, packed: 2.35 ms; 15 warps: 2.64 ms)
+constexpr int kAdjStreamWarps = 12;  // consumer warps (full electrode, packed: 2.35 ms; 10: 2.42 ms; 15: 2.64 ms)
 constexpr int kAdjStreamPlanes = 32;  // planes per work item
 constexpr int kAdjStreamMaxIpt = 4;
 constexpr int kAdjStreamSmemMax = 220 * 1024;
