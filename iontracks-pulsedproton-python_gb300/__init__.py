@@ -30,6 +30,7 @@ __all__ = [
     "ks_b200",
     "ks_and_gradient",
     "fit_alpha",
+    "fit_parameters",
     "AdjointRun",
 ]
 
@@ -45,7 +46,7 @@ def __getattr__(name):
         from . import batched
 
         return getattr(batched, name)
-    if name in ("ks_b200", "ks_and_gradient", "fit_alpha", "AdjointRun"):
+    if name in ("ks_b200", "ks_and_gradient", "fit_alpha", "fit_parameters", "AdjointRun"):
         from . import adjoint
 
         return getattr(adjoint, name)

@@ -490,3 +490,88 @@ def fit_alpha(configs, ks_target, alpha0: float, iterations: int = 8, checkpoint
         if abs(step) <= tol * abs(alpha):
             break
     return alpha, history
+
+
+FITTABLE = PARAMS[:5]  # shared by a chamber's configurations; V is each configuration's own
+
+
+def fit_parameters(configs, ks_target, names=("alpha",), start=None, iterations: int = 10,
+                   checkpoint_every: int = 64, dtype: str = "float32", tol: float = 1e-7, damping: float = 1e-3):
+    """Fit any of (alpha, mu+, mu-, D+, D-) to a k_s curve.
+
+    ``configs`` (e.g. one chamber at several voltages) and ``ks_target``
+    define ``L = sum_q (k_s(config_q; theta) - target_q)^2`` over parameters
+    ``names`` shared by all configurations (the rest of each configuration's
+    theta stays its own, alpha defaulting to the reference's). Each
+    iteration runs every configuration forward and backward -- the adjoint
+    gives the Jacobian ``J[q, p] = dk_s(config_q) / dtheta_p`` -- and takes a
+    Levenberg-Marquardt step in relative coordinates (theta_p (1 + x_p), so
+    that alpha ~ 1e-6 and mu ~ 1 are on one scale):
+    ``(J'^T J' + damping diag(J'^T J')) x = -J'^T r``, J' = J theta. A step that
+    raises the loss is retaken with ten times the damping.
+    ``start``: {name: value} (default: the first configuration's own values).
+    Returns ``(values, history)``: {name: fitted value}, [(values, loss)].
+    """
+    names = tuple(names)
+    for nm in names:
+        if nm not in FITTABLE:
+            raise ValueError(f"cannot fit {nm!r}: choose from {FITTABLE}")
+    idx = [PARAMS.index(nm) for nm in names]
+    target = np.asarray(ks_target, dtype=np.float64)
+    if len(target) != len(configs):
+        raise ValueError("one target k_s per configuration")
+    base = [base_parameters(c) for c in configs]
+    values = np.array([base[0][i] for i in idx], dtype=np.float64)
+    if start:
+        for k, nm in enumerate(names):
+            if nm in start:
+                values[k] = float(start[nm])
+
+    def evaluate(vals, with_grad):
+        ks = np.zeros(len(configs))
+        jac = np.zeros((len(configs), len(names)))
+        for q, cfg in enumerate(configs):
+            theta = base[q].copy()
+            theta[idx] = vals
+            if with_grad:
+                k, grad, _ = ks_and_gradient(cfg, theta, checkpoint_every, dtype)
+                jac[q] = grad[idx]
+            else:
+                run = AdjointRun(cfg, theta, checkpoint_every, dtype)
+                try:
+                    k = run.forward()
+                finally:
+                    run.release()
+            ks[q] = k
+        r = ks - target
+        return float(np.sum(r * r)), r, jac
+
+    loss, r, jac = evaluate(values, True)
+    history = [(dict(zip(names, values.tolist())), loss)]
+    lam = float(damping)
+    for _ in range(int(iterations)):
+        js = jac * values  # relative coordinates
+        a = js.T @ js
+        g = js.T @ r
+        accepted = False
+        for _retry in range(6):
+            x = np.linalg.solve(a + lam * np.diag(np.diag(a)), -g)
+            trial = values * (1.0 + x)
+            if np.any(trial <= 0.0):
+                lam *= 10.0
+                continue
+            t_loss, _, _ = evaluate(trial, False)
+            if t_loss <= loss:
+                accepted = True
+                break
+            lam *= 10.0
+        if not accepted:
+            break
+        step = np.max(np.abs(x))
+        values = trial
+        lam = max(lam / 10.0, 1e-12)
+        loss, r, jac = evaluate(values, True)
+        history.append((dict(zip(names, values.tolist())), loss))
+        if step <= tol:
+            break
+    return dict(zip(names, values.tolist())), history

@@ -399,3 +399,35 @@ def test_stream_variant_gradient(wall):
                                    shape={"variant": "stream", "adjoint_variant": "stream"})
     assert abs(ks1 - ks0) <= 1e-6
     np.testing.assert_allclose(g1, g0, rtol=1e-5)
+
+
+def test_fit_parameters_validates_its_names():
+    A = _adj()
+    cfg = make_config("column_10um_r02")
+    with pytest.raises(ValueError):
+        A.fit_parameters([cfg], [1.0], names=("voltage_V",))
+    with pytest.raises(ValueError):
+        A.fit_parameters([cfg, cfg], [1.0], names=("alpha",))
+
+
+@pytest.mark.gpu
+def test_fit_two_parameters_to_a_saturation_curve(oracle):
+    """Fit alpha and mu- together to a synthetic k_s(V) curve: the 10 um,
+    r = 0.02 cm column at 8 voltages over 50-400 V, targets from the float64
+    oracle at alpha x 1.3 and mu- x 0.85; Levenberg-Marquardt steps from the
+    float32 adjoint's Jacobian recover both from the reference values."""
+    A = _adj()
+    alpha0 = pkg().RECOMBINATION_ALPHA_CM3_S
+    volts = np.linspace(50.0, 400.0, 8)
+    cfgs = [make_config("column_10um_r02", voltage_V=float(v)) for v in volts]
+    true = {"alpha": 1.3 * alpha0, "mu_negative": 0.85 * cfgs[0].mu_negative}
+    target = []
+    for c in cfgs:
+        th = A.base_parameters(c, true["alpha"])
+        th[2] = true["mu_negative"]
+        target.append(oracle.run(A.config_at(c, th), mode="batched", alpha_cm3_s=th[0], threads=16,
+                                 keep_fields=False)["ks"])
+    values, history = A.fit_parameters(cfgs, target, names=("alpha", "mu_negative"), iterations=8)
+    assert values["alpha"] == pytest.approx(true["alpha"], rel=1e-3)
+    assert values["mu_negative"] == pytest.approx(true["mu_negative"], rel=1e-3)
+    assert history[-1][1] < 1e-6 * history[0][1]
