@@ -450,21 +450,24 @@ def run_gb300(args):
     del eng
     torch.cuda.empty_cache()
 
-    # end to end through the public solver call (host sampling, H2D tracks,
-    # D2H tallies), the same steps as the device-resident timing
+    # end to end through the public solver call (the pulse's schedule and
+    # track sampling on the host, H2D of tracks, D2H of tallies): by default
+    # the whole first pulse (every step depositing), over which the pulse's
+    # one-time host work is spread as it is in a run
     e2e = None
+    e2e_steps = int(args.e2e_steps) if args.e2e_steps > 0 else int(cfg.pulse_time_steps)
     if rank == 0 or world > 1:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         res = pkg.run_simulation_b200(cfg, rng=np.random.default_rng(replicas.replica_seed(cfg.seed, rank)),
-                                      progress=False, max_steps=args.e2e_steps, return_fields=False, shape=shape)
+                                      progress=False, max_steps=e2e_steps, return_fields=False, shape=shape)
         torch.cuda.synchronize()
         e2e_s = time.perf_counter() - t0
-        tracks = float(sched[: args.e2e_steps].sum())
+        tracks = float(sched[:e2e_steps].sum())  # the whole run's schedule
         e2e_rate = replicas.whole_job_rate(vox * res.steps_completed, e2e_s)
         e2e_s = replicas.max_over_ranks(e2e_s)
         e2e = {"value": e2e_rate, "unit": "voxel-steps/s",
-               "h2d_bytes_per_step": 16.0 * tracks / args.e2e_steps, "d2h_bytes_per_step": 32,
+               "h2d_bytes_per_step": 16.0 * tracks / e2e_steps, "d2h_bytes_per_step": 32,
                "steps": int(res.steps_completed), "wall_s": e2e_s,
                "includes": "schedule + track sampling on the host, H2D of tracks, all steps, D2H of tallies"}
 
@@ -518,7 +521,8 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["saturation_sweep", "adjoint", "adjoint_full_electrode"], default="full_electrode_5um")
     ap.add_argument("--dtype", choices=["float32", "float64"], default="float32")
-    ap.add_argument("--e2e-steps", type=int, default=600)
+    ap.add_argument("--e2e-steps", type=int, default=0,
+                    help="steps of the end-to-end run (0: the whole first pulse)")
     ap.add_argument("--cpu-steps", dest="cpu_steps", type=int, default=50,
                     help="pulse steps of the float64 oracle timed for the cpu_baseline (~0.2 s each at full size)")
     ap.add_argument("--ref-max-steps", dest="ref_max_steps", type=int, default=300,
