@@ -431,3 +431,30 @@ def test_fit_two_parameters_to_a_saturation_curve(oracle):
     assert values["alpha"] == pytest.approx(true["alpha"], rel=1e-3)
     assert values["mu_negative"] == pytest.approx(true["mu_negative"], rel=1e-3)
     assert history[-1][1] < 1e-6 * history[0][1]
+
+
+def test_binomial_schedule_on_long_runs_matches_the_closed_form():
+    """Longer runs (up to 5 000 steps, 2 to 12 slots): every adjoint step
+    once, in order, from its own state, and forward steps (spine + recomputed)
+    equal Griewank's closed form t l - beta(s+1, t-1) = t l - C(s+t, s+1), t
+    the fewest repetitions with C(s+t, s) >= l (s = 1: l (l-1) / 2)."""
+    from math import comb
+
+    def closed_form(l, s):
+        if l <= 1:
+            return 0
+        if s == 1:
+            return l * (l - 1) // 2
+        t = 0
+        while comb(s + t, s) < l:
+            t += 1
+        return t * l - comb(s + t, s + 1)
+
+    for n_steps, n_slots in [(97, 2), (500, 3), (1000, 5), (2500, 7), (5000, 12), (5000, 2)]:
+        ev, adv, spine = _trace(n_steps, n_slots)
+        adj = ev[ev[:, 0] == 2, 1]
+        assert np.array_equal(adj, np.arange(n_steps - 1, -1, -1)), (n_steps, n_slots)
+        assert adv + int(spine[-1]) == closed_form(n_steps, n_slots), (n_steps, n_slots)
+        # no advance starts past the run or runs off its end
+        adv_ev = ev[ev[:, 0] == 1]
+        assert np.all(adv_ev[:, 1] + adv_ev[:, 2] <= n_steps)
