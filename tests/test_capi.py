@@ -151,3 +151,26 @@ def test_launch_shape_resolution_without_a_gpu():
     wide = eng.make_grid(make_config("sweep_hi"), shape={"variant": "stream"})
     s = eng.resolve_shape(wide)
     assert s["stages"] >= 4
+
+
+def test_autotuner_candidates_are_shapes_the_library_accepts():
+    """Every streaming shape the quick autotuner would time on the full
+    electrode (and on a 10 um column) passes the library's own checks, wide
+    12-16-warp forms included (no GPU: shape resolution is host code)."""
+    import importlib
+
+    from goldens import make_config
+
+    eng = importlib.import_module(pkg().__name__ + ".engine")
+    at = importlib.import_module(pkg().__name__ + ".autotune")
+    native = importlib.import_module(pkg().__name__ + "._native")
+    for name in ("full_electrode_5um_10p", "column_10um_r02"):
+        g = eng.make_grid(make_config(name))
+        shapes = at.candidate_shapes(g, quick=True)
+        assert any(s.get("consumer_warps", 0) >= 12 for s in shapes) or g.no_xy < 64
+        for shape in shapes:
+            h = native.PicGrid.from_buffer_copy(g)
+            for k in eng.SHAPE_FIELDS:
+                setattr(h, k, 0)
+            eng.apply_shape(h, shape)
+            eng.resolve_shape(h)  # raises if the library refuses the shape
