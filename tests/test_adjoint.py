@@ -276,8 +276,8 @@ def test_full_electrode_gradient_in_180_gb():
     forward + adjoint of its first 100 steps (a track-depositing stretch of
     the first pulse) under a 180 GB device-memory limit -- the binomial
     schedule, with as many 3.7 GB state slots as fit -- against central
-    differences of float64 forward runs of the same 100 steps, for alpha,
-    mu- and V; peak device memory within the limit."""
+    differences of float64 forward runs of the same 100 steps, for all six
+    parameters; peak device memory within the limit."""
     import torch
 
     A = _adj()
@@ -308,7 +308,7 @@ def test_full_electrode_gradient_in_180_gb():
 
     k64 = fwd(theta)
     assert abs(ks - k64) <= 1e-6, (ks, k64)
-    for q in (0, 2, 5):
+    for q in range(6):
         tp, tmn = theta.copy(), theta.copy()
         tp[q] *= 1 + REL_STEP
         tmn[q] *= 1 - REL_STEP
