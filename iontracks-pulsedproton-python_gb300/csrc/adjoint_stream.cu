@@ -35,8 +35,12 @@ namespace pic {
 namespace {
 
 constexpr int kAdjStreamStages = 4;
-constexpr int kAdjStreamWarps = 12;  // consumer warps (full electrode, packed: 2.35 ms; 10: 2.42 ms; 15: 2.64 ms)
-constexpr int kAdjStreamPlanes = 32;  // planes per work item
+constexpr int kAdjStreamWarps = 12;  // consumer warps (full electrode, packed, 32-plane items: 2.35 ms; 10: 2.42 ms; 15: 2.64 ms)
+// Planes per work item: a longer item restarts the ring (two planes of
+// halo) less often -- 64 planes: 2.337 ms per full-electrode step, 32: 2.377
+// ms, 96: 2.341 ms, 128: 2.434 ms -- but leaves fewer items to balance over
+// the SMs, so 64 is taken only where every SM still gets kAdjStreamMinItems.
+constexpr int kAdjStreamPlanes = 64, kAdjStreamPlanesShort = 32, kAdjStreamMinItems = 16;
 constexpr int kAdjStreamMaxIpt = 4;
 constexpr int kAdjStreamSmemMax = 220 * 1024;
 
@@ -491,8 +495,10 @@ int launch_adjoint_stream(const pic_grid *g, const void *pos, const void *neg, c
     a.dp = (int)dens_pitch(g->no_xy);
     a.tj = tile_rows(a.n, a.kp);
     if (a.tj < 1) return set_error(PIC_E_CAPACITY, "adjoint stream variant: no tile fits shared memory");
-    a.li = kAdjStreamPlanes;
     a.jt = (a.n - 2 + a.tj - 1) / a.tj;
+    a.li = kAdjStreamPlanes;
+    if ((int64_t)a.jt * ((a.n - 2 + a.li - 1) / a.li) < (int64_t)kAdjStreamMinItems * sm_count())
+        a.li = kAdjStreamPlanesShort;
     a.n_items = a.jt * ((a.n - 2 + a.li - 1) / a.li);
     a.stages = kAdjStreamStages;
     a.consumer_warps = kAdjStreamWarps;

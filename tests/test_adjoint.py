@@ -340,24 +340,40 @@ def _adjoint_step(g, pos, neg, dens, lp, ln):
     return lp_out.cpu().numpy(), ln_out.cpu().numpy(), grad.cpu().numpy(), status
 
 
+# Grids of the streaming adjoint's kernel-level check: (config overrides,
+# tile rows, planes per work item).
+STREAM_ADJOINT_CASES = {
+    # the 10 um chamber at r = 0.035 cm: 14-row tiles, 32-plane items
+    "short_items": (dict(sampled_radius_cm=0.035), 14, 32),
+    # a thin chamber (no_z 8, kpitch 16) 1608 columns wide: 16-row tiles and
+    # 2 626 work items of 64 planes (at least 16 per SM on 152 SMs)
+    "long_items": (dict(sampled_radius_cm=0.8, electrode_gap_cm=0.008), 16, 64),
+}
+
+
 @pytest.mark.gpu
+@pytest.mark.parametrize("case", sorted(STREAM_ADJOINT_CASES))
 @pytest.mark.parametrize("wall", ["absorbing", "reflecting"])
 @pytest.mark.parametrize("deposit", [False, True])
-def test_stream_adjoint_step_equals_the_flat_one(wall, deposit):
+def test_stream_adjoint_step_equals_the_flat_one(case, wall, deposit):
     """pic_adjoint_step with the streaming kernel (adjoint_variant STREAM)
     against the flat kernel (adjoint_variant FLAT) on the same random state, lambda and
-    deposition pairs, on a grid whose tiles and work items are ragged (the
-    10 um chamber at r = 0.035 cm): lambda_s of every column, the ring's
+    deposition pairs, on grids whose tiles and work items are ragged, with
+    32- and 64-plane work items: lambda_s of every column, the ring's
     included, to 1e-6 of its scale; the step's five derivative sums to 1e-5
     relative."""
     import torch
 
     eng_mod = importlib.import_module(pkg().__name__ + ".engine")
     N = importlib.import_module(pkg().__name__ + "._native")
-    cfg = make_config("column_10um_r02", sampled_radius_cm=0.035, lateral_boundary=wall)
+    overrides, tile_rows, planes = STREAM_ADJOINT_CASES[case]
+    cfg = make_config("column_10um_r02", lateral_boundary=wall, **overrides)
     n, nzb = int(cfg.no_xy), int(cfg.no_z_with_buffer)
     kp = (nzb + 7) // 8 * 8
-    assert (n - 2) % 14 and (n - 2) % 32, n  # ragged last tile and last item
+    assert (n - 2) % tile_rows and (n - 2) % planes, n  # ragged last tile and last item
+    if planes == 64:
+        items = -(-(n - 2) // tile_rows) * -(-(n - 2) // 64)
+        assert kp == 16 and items >= 16 * torch.cuda.get_device_properties(0).multi_processor_count, items
     rng = np.random.default_rng(7)
     state = rng.uniform(0.0, 1e6, size=(2, n, n, kp)).astype(np.float32)
     state[..., 0] = 0.0
