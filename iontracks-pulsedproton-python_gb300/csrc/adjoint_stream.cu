@@ -35,7 +35,10 @@ namespace pic {
 namespace {
 
 constexpr int kAdjStreamStages = 4;
-constexpr int kAdjStreamWarps = 12;  // consumer warps (full electrode, packed, 32-plane items: 2.35 ms; 10: 2.42 ms; 15: 2.64 ms)
+// consumer warps; full electrode, packed, 32-plane items: 12 warps 2.35 ms,
+// 10: 2.42 ms, 15: 2.64 ms; 64-plane items: 12 warps 2.34 ms, 13: 2.60 ms,
+// 14: 2.59 ms
+constexpr int kAdjStreamWarps = 12;
 // Planes per work item: a longer item restarts the ring (two planes of
 // halo) less often -- 64 planes: 2.337 ms per full-electrode step, 32: 2.377
 // ms, 96: 2.341 ms, 128: 2.434 ms -- but leaves fewer items to balance over
