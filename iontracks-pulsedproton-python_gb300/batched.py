@@ -166,12 +166,20 @@ def run_batched_b200(
     """
     import torch
 
+    n_cfg = len(configs)
+    if rngs is not None and len(rngs) != n_cfg:
+        raise ValueError(f"rngs holds {len(rngs)} generators for {n_cfg} configurations")
+    if dtype not in ("float32", "float64"):
+        raise ValueError(f"dtype must be 'float32' or 'float64', got {dtype!r}")
+    if int(chunk_steps) < 1:
+        raise ValueError("chunk_steps must be >= 1")
+    if int(solo_grids) < 0:
+        raise ValueError("solo_grids must be >= 0")
     if not torch.cuda.is_available():
         raise RuntimeError("run_batched_b200 needs a CUDA device (a GB300); none is visible")
     lib = N.load()
     sms = N.device_info()[0]
     dev = torch.device("cuda", torch.cuda.current_device())
-    n_cfg = len(configs)
     if n_cfg == 0:
         return []
     tdt = torch.float32 if dtype == "float32" else torch.float64

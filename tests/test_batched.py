@@ -47,6 +47,20 @@ def test_phases_cover_every_step_once():
     assert ph == [(0, 3, [0, 1, 2, 3]), (3, 5, [0, 2, 3]), (5, 9, [3])]
 
 
+@pytest.mark.parametrize("kw, msg", [
+    (dict(rngs=[np.random.default_rng(1)]), "1 generators for 2 configurations"),
+    (dict(dtype="float16"), "dtype must be"),
+    (dict(chunk_steps=0), "chunk_steps must be >= 1"),
+    (dict(solo_grids=-1), "solo_grids must be >= 0"),
+])
+def test_batched_arguments_checked_before_device_work(kw, msg):
+    """Inconsistent arguments are refused before any device work (and here,
+    without a GPU): one generator per configuration, a known dtype, positive
+    chunks."""
+    with pytest.raises(ValueError, match=msg):
+        pkg().run_batched_b200([make_config("fast"), make_config("small_run")], **kw)
+
+
 @pytest.mark.gpu
 def test_batched_matches_individual_runs():
     cfgs = _mixed_batch()
