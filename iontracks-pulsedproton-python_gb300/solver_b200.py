@@ -91,6 +91,8 @@ def run_simulation_b200(
     """
     if dtype not in ("float32", "float64"):
         raise ValueError(f"dtype must be 'float32' or 'float64', got {dtype!r}")
+    if int(chunk_steps) < 1:
+        raise ValueError("chunk_steps must be >= 1")
     total = int(config.total_time_steps)
     last_step = total if max_steps is None else max(0, min(total, int(max_steps)))
     rng = rng if rng is not None else np.random.default_rng(config.seed)

@@ -116,6 +116,30 @@ def test_grid_descriptor_from_config():
         eng.make_grid(cfg, dtype="float16")
 
 
+def test_public_calls_fail_loudly_without_a_gpu():
+    """No CPU fallback: every public entry point refuses to run without a
+    CUDA device (and refuses bad arguments before looking for one)."""
+    import torch
+
+    from goldens import make_config
+
+    P = pkg()
+    cfg = make_config("fast")
+    with pytest.raises(ValueError, match="chunk_steps"):
+        P.run_simulation_b200(cfg, progress=False, chunk_steps=0)
+    if torch.cuda.is_available():
+        pytest.skip("checks the behaviour without a GPU")
+    calls = [
+        lambda: P.run_simulation_b200(cfg, progress=False),
+        lambda: P.run_batched_b200([cfg]),
+        lambda: P.ks_and_gradient(cfg),
+        lambda: P.fit_parameters([cfg, cfg], [1.01, 1.02], names=("alpha",)),
+    ]
+    for call in calls:
+        with pytest.raises(RuntimeError, match="needs a CUDA device"):
+            call()
+
+
 def test_launch_shape_resolution_without_a_gpu():
     import importlib
 
