@@ -41,9 +41,11 @@ constexpr int kAdjStreamStages = 4;
 constexpr int kAdjStreamWarps = 12;
 // Planes per work item: a longer item restarts the ring (two planes of
 // halo) less often -- 64 planes: 2.337 ms per full-electrode step, 32: 2.377
-// ms, 96: 2.341 ms, 128: 2.434 ms -- but leaves fewer items to balance over
-// the SMs, so 64 is taken only where every SM still gets kAdjStreamMinItems.
-constexpr int kAdjStreamPlanes = 64, kAdjStreamPlanesShort = 32, kAdjStreamMinItems = 16;
+// ms, 96: 2.341 ms, 128: 2.434 ms; on 608 x 608 x 406 (6.6 items of 64
+// planes per SM) 0.788 against 0.794 ms -- but leaves fewer items to balance
+// over the SMs, so 64 is taken only where every SM still gets
+// kAdjStreamMinItems.
+constexpr int kAdjStreamPlanes = 64, kAdjStreamPlanesShort = 32, kAdjStreamMinItems = 6;
 constexpr int kAdjStreamMaxIpt = 4;
 constexpr int kAdjStreamSmemMax = 220 * 1024;
 

@@ -346,7 +346,7 @@ STREAM_ADJOINT_CASES = {
     # the 10 um chamber at r = 0.035 cm: 14-row tiles, 32-plane items
     "short_items": (dict(sampled_radius_cm=0.035), 14, 32),
     # a thin chamber (no_z 8, kpitch 16) 1608 columns wide: 16-row tiles and
-    # 2 626 work items of 64 planes (at least 16 per SM on 152 SMs)
+    # 2 626 work items of 64 planes (at least 6 per SM on 152 SMs)
     "long_items": (dict(sampled_radius_cm=0.8, electrode_gap_cm=0.008), 16, 64),
 }
 
@@ -373,7 +373,7 @@ def test_stream_adjoint_step_equals_the_flat_one(case, wall, deposit):
     assert (n - 2) % tile_rows and (n - 2) % planes, n  # ragged last tile and last item
     if planes == 64:
         items = -(-(n - 2) // tile_rows) * -(-(n - 2) // 64)
-        assert kp == 16 and items >= 16 * torch.cuda.get_device_properties(0).multi_processor_count, items
+        assert kp == 16 and items >= 6 * torch.cuda.get_device_properties(0).multi_processor_count, items
     rng = np.random.default_rng(7)
     state = rng.uniform(0.0, 1e6, size=(2, n, n, kp)).astype(np.float32)
     state[..., 0] = 0.0
