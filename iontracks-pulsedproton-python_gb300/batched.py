@@ -140,6 +140,55 @@ def _phases(total_steps: Sequence[int]):
     return phases
 
 
+def _task_tables(offsets, totals, track_base):
+    """The deposition tasks of every global step, in grid order within a step.
+
+    ``offsets[c]`` = grid c's cumulative track counts per step (length
+    ``totals[c] + 1``), ``track_base[c]`` = its first track in the packed
+    track arrays. Returns ``(step_task_off, step_tracks, task_cfg,
+    task_first, task_prefix)``: the tasks of step s are ``step_task_off[s] ..
+    step_task_off[s + 1] - 1``, one per grid with tracks at s, giving the
+    grid, its first packed track and the tracks of the step's earlier tasks
+    (one warp group per track, so the warps before it); ``step_tracks[s]`` =
+    all tracks of step s."""
+    n_cfg = len(offsets)
+    S = max(totals)
+    M = np.zeros((S, n_cfg), dtype=np.int64)  # tracks of grid c at global step s
+    F = np.zeros((S, n_cfg), dtype=np.int64)  # first track of (s, c) in the packed arrays
+    for c in range(n_cfg):
+        M[: totals[c], c] = np.diff(offsets[c])
+        F[: totals[c], c] = track_base[c] + offsets[c][:-1]
+    s_idx, c_idx = np.nonzero(M)  # row-major: by step, then grid
+    vals = M[s_idx, c_idx]
+    step_task_off = np.zeros(S + 1, dtype=np.int64)
+    np.cumsum(np.bincount(s_idx, minlength=S), out=step_task_off[1:])
+    step_tracks = M.sum(axis=1)
+    excl = np.cumsum(vals) - vals  # tracks before each task, over all steps
+    t_prefix = excl - excl[step_task_off[s_idx]] if len(vals) else excl
+    return step_task_off, step_tracks, c_idx.astype(np.int32), F[s_idx, c_idx], t_prefix
+
+
+def _work_table(items, active, sms: int) -> dict:
+    """Blocks of one batched launch over the ``active`` grids (``items[c]`` =
+    grid c's work items): each grid gets contiguous blocks, and block b of a
+    grid with nb blocks steps its items [b it / nb, (b + 1) it / nb)."""
+    items = np.asarray(items, dtype=np.int64)
+    act = np.asarray(active, dtype=np.int64)
+    n_cfg = len(items)
+    ipb = items_per_block(int(items[act].sum()), sms)
+    nb = np.maximum(1, -(-items[act] // ipb))
+    first = np.concatenate([[0], np.cumsum(nb)[:-1]])
+    cfg_blk0 = np.zeros(n_cfg, dtype=np.int32)
+    cfg_nblk = np.zeros(n_cfg, dtype=np.int32)
+    cfg_blk0[act] = first
+    cfg_nblk[act] = nb
+    blk_cfg = np.repeat(act, nb)
+    b = np.arange(int(nb.sum()), dtype=np.int64) - np.repeat(first, nb)  # block index within its grid
+    it, nbr = items[blk_cfg], np.repeat(nb, nb)
+    return dict(blk_cfg=blk_cfg.astype(np.int32), blk_item0=b * it // nbr, blk_item1=(b + 1) * it // nbr,
+                cfg_blk0=cfg_blk0, cfg_nblk=cfg_nblk)
+
+
 def run_batched_b200(
     configs: Sequence,
     rngs: Optional[Sequence[np.random.Generator]] = None,
@@ -242,21 +291,9 @@ def run_batched_b200(
     ys_dev = torch.zeros(max(base, 1), dtype=torch.float64, device=dev)
 
     # --- per global step: tasks (grid, first track, first warp), in grid
-    # order within a step; M[s, c] = tracks of grid c at global step s
+    # order within a step
     S = max(totals)
-    M = np.zeros((S, n_cfg), dtype=np.int64)
-    F = np.zeros((S, n_cfg), dtype=np.int64)  # first track of (s, c) in the packed arrays
-    for c in range(n_cfg):
-        M[: totals[c], c] = np.diff(offsets[c])
-        F[: totals[c], c] = track_base[c] + offsets[c][:-1]
-    s_idx, c_idx = np.nonzero(M)  # row-major: by step, then grid
-    vals = M[s_idx, c_idx]
-    step_task_off = np.zeros(S + 1, dtype=np.int64)
-    np.cumsum(np.bincount(s_idx, minlength=S), out=step_task_off[1:])
-    step_tracks = M.sum(axis=1)
-    excl = np.cumsum(vals) - vals  # warps before each task, over all steps
-    t_prefix = excl - excl[step_task_off[s_idx]] if len(vals) else excl
-    t_cfg, t_first = c_idx.astype(np.int32), F[s_idx, c_idx]
+    step_task_off, step_tracks, t_cfg, t_first, t_prefix = _task_tables(offsets, totals, track_base)
     one = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a if len(a) else np.zeros(1), dtype=dt)).to(dev)
     task_cfg = one(t_cfg, np.int32)
     task_first = one(t_first, np.int64)
@@ -265,29 +302,13 @@ def run_batched_b200(
     # --- work tables, one per set of active grids
     phases = []
     max_blocks = 1
-    items_a = np.asarray(items, dtype=np.int64)
     for s0, s1, active in _phases(totals):
-        act = np.asarray(active, dtype=np.int64)
-        ipb = items_per_block(int(items_a[act].sum()), sms)
-        nb = np.maximum(1, -(-items_a[act] // ipb))
-        first = np.concatenate([[0], np.cumsum(nb)[:-1]])
-        cfg_blk0 = np.zeros(n_cfg, dtype=np.int32)
-        cfg_nblk = np.zeros(n_cfg, dtype=np.int32)
-        cfg_blk0[act] = first
-        cfg_nblk[act] = nb
-        blk_cfg = np.repeat(act, nb)
-        b = np.arange(int(nb.sum()), dtype=np.int64) - np.repeat(first, nb)  # block index within its grid
-        it, nbr = items_a[blk_cfg], np.repeat(nb, nb)
-        i0, i1 = b * it // nbr, (b + 1) * it // nbr
-        max_blocks = max(max_blocks, len(blk_cfg))
+        wt = _work_table(items, active, sms)
+        max_blocks = max(max_blocks, len(wt["blk_cfg"]))
         phases.append((s0, s1, dict(
-            active=[int(c) for c in act],
-            blk_cfg=torch.from_numpy(blk_cfg.astype(np.int32)).to(dev),
-            blk_item0=torch.from_numpy(i0).to(dev),
-            blk_item1=torch.from_numpy(i1).to(dev),
-            cfg_blk0=torch.from_numpy(cfg_blk0).to(dev),
-            cfg_nblk=torch.from_numpy(cfg_nblk).to(dev),
-            n_blocks=int(len(blk_cfg)),
+            active=[int(c) for c in active],
+            n_blocks=int(len(wt["blk_cfg"])),
+            **{k: torch.from_numpy(v).to(dev) for k, v in wt.items()},
         )))
     # 32-bit offsets when every grid's fields are < 2^31 elements
     index32 = all(int(g.no_xy) <= 16383 and int(g.no_xy) ** 2 * int(g.kpitch) < 2**31 for g in grids)

@@ -47,6 +47,66 @@ def test_phases_cover_every_step_once():
     assert ph == [(0, 3, [0, 1, 2, 3]), (3, 5, [0, 2, 3]), (5, 9, [3])]
 
 
+def _ragged_schedules(rng, n):
+    totals = [int(rng.integers(1, 60)) for _ in range(n)]
+    offsets, base, b = [], [], 0
+    for t in totals:
+        sched = rng.integers(0, 5, size=t) * (rng.uniform(size=t) < 0.4)
+        off = np.zeros(t + 1, dtype=np.int64)
+        np.cumsum(sched, out=off[1:])
+        offsets.append(off)
+        base.append(b)
+        b += int(off[-1])
+    return offsets, totals, base
+
+
+def test_deposition_tasks_of_every_global_step():
+    """Per global step, one task per grid with tracks, in grid order: its
+    grid, first packed track and the tracks of the step's earlier tasks."""
+    import importlib
+
+    b = importlib.import_module(pkg().__name__ + ".batched")
+    rng = np.random.default_rng(9)
+    for _ in range(50):
+        offsets, totals, base = _ragged_schedules(rng, int(rng.integers(1, 8)))
+        sto, stt, cfg, first, prefix = b._task_tables(offsets, totals, base)
+        assert len(sto) == max(totals) + 1 and sto[0] == 0 and sto[-1] == len(cfg)
+        for s in range(max(totals)):
+            want = [(c, base[c] + offsets[c][s], offsets[c][s + 1] - offsets[c][s])
+                    for c in range(len(totals)) if s < totals[c] and offsets[c][s + 1] > offsets[c][s]]
+            got = range(sto[s], sto[s + 1])
+            assert [(cfg[t], first[t]) for t in got] == [(c, f) for c, f, _ in want]
+            assert [prefix[t] for t in got] == list(np.cumsum([0] + [m for _, _, m in want])[:-1])
+            assert stt[s] == sum(m for _, _, m in want)
+
+
+def test_work_tables_cover_each_active_grid_once():
+    """One batched launch's blocks: every active grid's items split into
+    contiguous, non-overlapping block ranges covering them exactly; inactive
+    grids get no blocks."""
+    import importlib
+
+    b = importlib.import_module(pkg().__name__ + ".batched")
+    rng = np.random.default_rng(4)
+    for _ in range(200):
+        n = int(rng.integers(1, 9))
+        items = rng.integers(1, 3_000_000, size=n)
+        active = sorted(rng.choice(n, size=int(rng.integers(1, n + 1)), replace=False).tolist())
+        wt = b._work_table(items, active, int(rng.integers(1, 200)))
+        assert wt["blk_cfg"].dtype == np.int32 and wt["cfg_blk0"].dtype == np.int32
+        for c in range(n):
+            b0, nb = int(wt["cfg_blk0"][c]), int(wt["cfg_nblk"][c])
+            if c not in active:
+                assert nb == 0
+                continue
+            blocks = range(b0, b0 + nb)
+            assert nb >= 1 and all(wt["blk_cfg"][k] == c for k in blocks)
+            i0, i1 = wt["blk_item0"][b0:b0 + nb], wt["blk_item1"][b0:b0 + nb]
+            assert i0[0] == 0 and i1[-1] == items[c] and np.array_equal(i0[1:], i1[:-1])
+            assert np.all(i1 > i0) or items[c] < nb
+        assert len(wt["blk_cfg"]) == int(wt["cfg_nblk"].sum())
+
+
 @pytest.mark.parametrize("kw, msg", [
     (dict(rngs=[np.random.default_rng(1)]), "1 generators for 2 configurations"),
     (dict(dtype="float16"), "dtype must be"),
