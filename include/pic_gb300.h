@@ -182,12 +182,25 @@ int pic_step(const pic_grid *g, const void *pos_in, const void *neg_in, void *po
  * 1448 for float32 fields, <= 1024 for float64 -- else PIC_E_CAPACITY. Every
  * GPU that loads the library holds the array (16 MiB plus the tally workspace)
  * until exit. All calls share it: calls that overlap on the GPU race, so
- * serialise them. The first call on a device looks up the array's device
- * address; make it before any stream capture.
+ * serialise them. Each call looks up the array's device address on the
+ * current device (so it stays right after a device reset); the first call on
+ * a device also loads the library's device code there: make it before any
+ * stream capture.
  */
 int pic_step_noalloc(const pic_grid *g, const void *pos_in, const void *neg_in, void *pos_out, void *neg_out,
                      const double *xs, const double *ys, int64_t n_tracks, uint32_t *counts, double *tally,
                      uintptr_t stream);
+
+/*
+ * pic_step_noalloc_status -- the status word of pic_step_noalloc's static
+ * workspace: 0, or the code of a bounded wait of the streaming step that ran
+ * out (the fields of that step are then wrong). Waits for `stream` first.
+ * With reset != 0 it also clears the word and the tally completion counter.
+ * Allocates nothing. No counterpart in the reference; it exists because the
+ * caller of pic_step_noalloc never sees the workspace that pic_workspace_status
+ * would need.
+ */
+int pic_step_noalloc_status(int32_t reset, uintptr_t stream, int32_t *status);
 
 /*
  * pic_sample_disc -- the rejection step of the host track sampler (no GPU).

@@ -361,6 +361,11 @@ int pic_step_noalloc(const pic_grid *g, const void *pos_in, const void *neg_in, 
                         reinterpret_cast<cudaStream_t>(stream));
 }
 
+int pic_step_noalloc_status(int32_t reset, uintptr_t stream, int32_t *status) {
+    if (!status) return set_error(PIC_E_INVALID, "status is null");
+    return step_noalloc_status(reset, reinterpret_cast<cudaStream_t>(stream), status);
+}
+
 int pic_sample_disc(const double *u, int64_t n_pairs, double scale, double mid, double radius_sq, int64_t n_wanted,
                     double *xs, double *ys, int64_t *n_accepted, int64_t *n_pairs_used) {
     if (n_pairs < 0 || n_wanted < 0) return set_error(PIC_E_INVALID, "n_pairs and n_wanted must be >= 0");

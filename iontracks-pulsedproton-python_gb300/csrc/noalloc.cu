@@ -20,16 +20,22 @@
 //     workspace) until the process exits;
 //   * every call shares the array and it keeps the last call's contents: the
 //     pairs are cleared at the start of each call, the tally counter is
-//     left at zero by each completed step;
+//     left at zero by each step (an aborted one included: every block of the
+//     step still takes part in the tally reduction);
 //   * calls that overlap on the GPU (different streams, or different host
 //     threads) race on the array and give wrong results: serialise them;
-//   * the first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress) with that device current; make that first call
-//     before any stream capture.
+//   * each call looks up the array's device address (cudaGetSymbolAddress)
+//     with the caller's device current, so the address is right again after a
+//     cudaDeviceReset; the first call on a device also loads the library's
+//     device code there, so make it before any stream capture;
+//   * the streaming step waits on its copy ring with bounded waits; if one
+//     runs out it records a code in the array's status word and the step's
+//     fields are wrong. pic_step_noalloc_status reads that word (and, asked
+//     to, clears it together with the tally counter); a caller checks it
+//     after a run of steps.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include <mutex>
 #include <string>
 
 #include "pic_internal.h"
@@ -43,23 +49,16 @@ constexpr int64_t kNoAllocScratchBytes = kNoAllocDensBytes + kWorkspaceBytes;
 // workspace].
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-// Device address of the array, looked up once per device with that device
-// current (the host-side symbol is only a stand-in, not a device address).
+// Device address of the array on the current device. Looked up on every call
+// (a host-side lookup once the module is loaded) rather than cached, so that
+// a device reset, which may load the module at another address, cannot leave
+// a stale pointer behind. The host-side symbol is only a stand-in, not a
+// device address.
 static int noalloc_scratch(void **out) {
-    static std::mutex mu;
-    static void *addr[64] = {nullptr};
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return set_cuda_error("cudaGetDevice", e);
-    if (dev < 0 || dev >= 64) return set_error(PIC_E_DEVICE, "device ordinal out of range");
-    std::lock_guard<std::mutex> lock(mu);
-    if (!addr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return set_cuda_error("cudaGetSymbolAddress(g_noalloc_scratch)", e);
-        addr[dev] = p;
-    }
-    *out = addr[dev];
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return set_cuda_error("cudaGetSymbolAddress(g_noalloc_scratch)", e);
+    *out = p;
     return PIC_OK;
 }
 
@@ -86,6 +85,28 @@ int step_noalloc(const pic_grid *g, const void *pos_in, const void *neg_in, void
         if (rc) return rc;
     }
     return launch_step(g, pos_in, neg_in, pos_out, neg_out, n_tracks > 0 ? dens : nullptr, nullptr, tally, ws, st);
+}
+
+// Reads the status word of the array's tally workspace (0 = ok, else the code
+// of the bounded wait that ran out), after the stream's work so far; with
+// reset, clears it and the completion counter.
+int step_noalloc_status(int32_t reset, cudaStream_t st, int32_t *status) {
+    void *base = nullptr;
+    int rc = noalloc_scratch(&base);
+    if (rc) return rc;
+    Workspace w = workspace_layout(static_cast<unsigned char *>(base) + kNoAllocDensBytes);
+    int32_t v = 0;
+    cudaError_t e = cudaMemcpyAsync(&v, w.status, sizeof(v), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return set_cuda_error("pic_step_noalloc_status", e);
+    *status = v;
+    if (reset) {
+        e = cudaMemsetAsync(w.status, 0, sizeof(int32_t), st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(w.counter, 0, sizeof(unsigned int), st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return set_cuda_error("pic_step_noalloc_status reset", e);
+    }
+    return PIC_OK;
 }
 
 }  // namespace pic

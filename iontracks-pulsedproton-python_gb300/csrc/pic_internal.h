@@ -145,6 +145,7 @@ int launch_multistep(const pic_grid *g, void *const pos[2], void *const neg[2], 
 int step_noalloc(const pic_grid *g, const void *pos_in, const void *neg_in, void *pos_out, void *neg_out,
                  const double *xs, const double *ys, int64_t n_tracks, uint32_t *counts, double *tally,
                  cudaStream_t st);
+int step_noalloc_status(int32_t reset, cudaStream_t st, int32_t *status);
 
 int adjoint_workspace_bytes(int64_t *bytes);
 int launch_adjoint(const pic_grid *g, const void *pos, const void *neg, const void *dens, void *lp_in, void *ln_in,

@@ -100,6 +100,14 @@ def test_invalid_grid_is_refused_before_any_device_work(lib):
     assert rc == native.PIC_E_INVALID
 
 
+def test_noalloc_status_refuses_a_null_status_before_device_work(lib):
+    import importlib
+
+    native = importlib.import_module(pkg().__name__ + "._native")
+    assert lib.pic_step_noalloc_status(0, None, None) == native.PIC_E_INVALID
+    assert b"status is null" in lib.pic_last_error()
+
+
 def test_grid_descriptor_from_config():
     import importlib
 

@@ -8,7 +8,10 @@ static device array inside the library. This test checks that two calls in a
 row give what the allocating entry points (pic_deposit + pic_step with
 caller-allocated scratch) give on the same inputs, within the float32 parity
 tolerance of the other tests (1e-5), and that a grid too large for the static
-scratch is refused.
+scratch is refused. The cases cover both step kernels (the flat one and the
+streaming one, whose copies read the deposition from the static array) and
+the status word of the static workspace, read and cleared through
+pic_step_noalloc_status.
 
 Kept in a file of its own that is collected last, so that a run that stops at
 the first failure has already run every other test; it runs the same alone in
@@ -41,14 +44,30 @@ def _two_steps_of_tracks(cfg):
     return [(xs[: counts[0]], ys[: counts[0]]), (xs[counts[0]:], ys[counts[0]:])]
 
 
-@pytest.mark.parametrize("dtype, wall", [("float32", "absorbing"), ("float32", "reflecting"), ("float64", "absorbing")])
-def test_two_calls_match_the_allocating_entry_points(dtype, wall):
+# The grid (208 x 208 x 406, 1.8e7 cells) is below the size from which the
+# library picks the streaming step by itself, so the flat step runs unless a
+# case asks for the streaming one: its bulk copies then read the deposition
+# pairs out of the static array.
+CASES = [
+    ("float32", "absorbing", None),
+    ("float32", "reflecting", None),
+    ("float64", "absorbing", None),
+    ("float32", "absorbing", {"variant": "stream"}),
+    ("float32", "reflecting", {"variant": "stream", "tile_rows": 12, "consumer_warps": 15, "stages": 5}),
+]
+
+
+@pytest.mark.parametrize("dtype, wall, shape", CASES, ids=["f32-abs-flat", "f32-refl-flat", "f64-abs-flat",
+                                                           "f32-abs-stream", "f32-refl-stream15"])
+def test_two_calls_match_the_allocating_entry_points(dtype, wall, shape):
     import torch
 
     N, eng = _mods()
     lib = N.load()
     cfg = make_config("column_5um_r05_d89p1", lateral_boundary=wall)
-    g = eng.make_grid(cfg, dtype=dtype)
+    g = eng.make_grid(cfg, dtype=dtype, shape=shape)
+    if shape:
+        assert eng.resolve_shape(g)["variant"] == "stream"
     tdt = torch.float32 if dtype == "float32" else torch.float64
     shape = (g.no_xy, g.no_xy, g.kpitch)
     dev = torch.device("cuda")
@@ -91,6 +110,13 @@ def test_two_calls_match_the_allocating_entry_points(dtype, wall):
             np.testing.assert_allclose(b, a, rtol=0, atol=REL * peak)
         np.testing.assert_array_equal(counts_b.cpu().numpy(), counts_a.cpu().numpy())
         np.testing.assert_allclose(tally_b[s].cpu().numpy(), tally_a[s].cpu().numpy(), rtol=REL)
+    # no bounded wait ran out: the static workspace's status word reads 0,
+    # and reading it with reset leaves it 0
+    status = ctypes.c_int32(-1)
+    N.check(lib.pic_step_noalloc_status(1, stream, ctypes.byref(status)), "pic_step_noalloc_status")
+    assert status.value == 0
+    N.check(lib.pic_step_noalloc_status(0, stream, ctypes.byref(status)), "pic_step_noalloc_status")
+    assert status.value == 0
 
 
 def test_grid_beyond_the_static_scratch_is_refused():
