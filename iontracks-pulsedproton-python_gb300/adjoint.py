@@ -53,7 +53,7 @@ import numpy as np
 
 from . import _native as N
 from .config import lax_wendroff_weights
-from .constants import RECOMBINATION_ALPHA_CM3_S
+from .constants import recombination_alpha
 from .engine import ChamberEngine
 from .pulses import TrackSampler, build_track_schedule
 from .state import collection_efficiency
@@ -63,7 +63,7 @@ PARAMS = ("alpha", "mu_positive", "mu_negative", "D_positive", "D_negative", "vo
 
 def base_parameters(config, alpha_cm3_s: Optional[float] = None) -> np.ndarray:
     """``theta = (alpha, mu+, mu-, D+, D-, V)`` of a configuration."""
-    alpha = RECOMBINATION_ALPHA_CM3_S if alpha_cm3_s is None else float(alpha_cm3_s)
+    alpha = recombination_alpha(config) if alpha_cm3_s is None else float(alpha_cm3_s)
     return np.array([alpha, config.mu_positive, config.mu_negative, config.D_positive, config.D_negative,
                      config.voltage_V], dtype=np.float64)
 

@@ -15,7 +15,7 @@ import ctypes
 import numpy as np
 
 from . import _native as N
-from .constants import RECOMBINATION_ALPHA_CM3_S
+from .constants import recombination_alpha
 
 _DTYPES = {"float32": N.PIC_F32, "float64": N.PIC_F64}
 _VARIANTS = {"auto": N.PIC_VARIANT_AUTO, "flat": N.PIC_VARIANT_FLAT, "stream": N.PIC_VARIANT_STREAM}
@@ -52,7 +52,7 @@ def make_grid(config, dtype: str = "float32", alpha_cm3_s: float | None = None, 
     if dtype not in _DTYPES:
         raise ValueError(f"dtype must be 'float32' or 'float64', got {dtype!r}")
     (p_lat, p_zm, p_zp, p_cen), (n_lat, n_zm, n_zp, n_cen) = config.scheme_coefficients()
-    alpha = RECOMBINATION_ALPHA_CM3_S if alpha_cm3_s is None else float(alpha_cm3_s)
+    alpha = recombination_alpha(config) if alpha_cm3_s is None else float(alpha_cm3_s)
     g = N.PicGrid()
     g.no_xy = int(config.no_xy)
     g.nzb = int(config.no_z_with_buffer)
