@@ -27,7 +27,7 @@ import numpy as np
 
 from . import _native as N
 from .config import SimulationConfig
-from .engine import make_grid
+from .engine import make_grid, nvtx_range
 from .feeder import TrackFeeder
 from .pulses import TrackSampler, build_track_schedule
 from .state import Diagnostics, collection_efficiency
@@ -366,8 +366,9 @@ def run_batched_b200(
             # draw the next chunk's tracks while the device runs this one
             pending = feeder.submit(jobs_of(*chunks[k + 1][:2])) if k + 1 < len(chunks) else None
             if solo_ws is not None and len(tab["active"]) <= solo_grids:
-                for c in tab["active"]:  # independent grids: one after the other
-                    run_solo(c, c0, c1)
+                with nvtx_range(f"solo grids ({len(tab['active'])})"):
+                    for c in tab["active"]:  # independent grids: one after the other
+                        run_solo(c, c0, c1)
                 if progress:
                     print(f"  global step {c1}/{S}")
                 continue
@@ -394,11 +395,12 @@ def run_batched_b200(
             L.first_step, L.n_steps = c0, c1 - c0
             L.counts, L.tally = counts.data_ptr(), tally.data_ptr()
             L.workspace, L.workspace_bytes = workspace.data_ptr(), workspace.numel()
-            if persistent:
-                N.check(lib.pic_batched_persistent(ctypes.byref(L), sto_dev.data_ptr(), stt_dev.data_ptr(), st),
-                        "pic_batched_persistent")
-            else:
-                N.check(lib.pic_batched_segment(ctypes.byref(L), st), "pic_batched_segment")
+            with nvtx_range(f"batched steps ({len(tab['active'])} grids)"):
+                if persistent:
+                    N.check(lib.pic_batched_persistent(ctypes.byref(L), sto_dev.data_ptr(), stt_dev.data_ptr(), st),
+                            "pic_batched_persistent")
+                else:
+                    N.check(lib.pic_batched_segment(ctypes.byref(L), st), "pic_batched_segment")
             if progress:
                 print(f"  global step {c1}/{S}")
         torch.cuda.synchronize(dev)

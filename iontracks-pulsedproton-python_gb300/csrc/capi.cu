@@ -325,6 +325,7 @@ int pic_resolve_shape(const pic_grid *g, pic_grid *resolved) {
 
 int pic_deposit(const pic_grid *g, const double *xs, const double *ys, int64_t n_tracks, void *dens,
                 uint32_t *counts, uintptr_t stream) {
+    NvtxRange nvtx_range("pic_deposit");
     int rc = check_grid(g);
     if (rc) return rc;
     if (n_tracks < 0) return set_error(PIC_E_INVALID, "n_tracks must be >= 0");
@@ -336,6 +337,7 @@ int pic_deposit(const pic_grid *g, const double *xs, const double *ys, int64_t n
 int pic_step(const pic_grid *g, const void *pos_in, const void *neg_in, void *pos_out, void *neg_out,
              const void *dens, void *dens_zero, double *tally, void *workspace, int64_t workspace_bytes,
              uintptr_t stream) {
+    NvtxRange nvtx_range("pic_step");
     int rc = check_grid(g);
     if (rc) return rc;
     if ((rc = check_fields(pos_in, neg_in, pos_out, neg_out))) return rc;
@@ -350,6 +352,7 @@ int pic_step(const pic_grid *g, const void *pos_in, const void *neg_in, void *po
 int pic_step_noalloc(const pic_grid *g, const void *pos_in, const void *neg_in, void *pos_out, void *neg_out,
                      const double *xs, const double *ys, int64_t n_tracks, uint32_t *counts, double *tally,
                      uintptr_t stream) {
+    NvtxRange nvtx_range("pic_step_noalloc");
     int rc = check_grid(g);
     if (rc) return rc;
     if ((rc = check_fields(pos_in, neg_in, pos_out, neg_out))) return rc;
@@ -403,6 +406,7 @@ int pic_adjoint_workspace_bytes(const pic_grid *g, int64_t *bytes) {
 int pic_adjoint_step(const pic_grid *g, const void *pos, const void *neg, const void *dens, void *lam_pos_in,
                      void *lam_neg_in, void *lam_pos_out, void *lam_neg_out, double *grad, void *workspace,
                      int64_t workspace_bytes, uintptr_t stream) {
+    NvtxRange nvtx_range("pic_adjoint_step");
     int rc = check_grid(g);
     if (rc) return rc;
     if ((rc = check_fields(pos, neg, lam_pos_in, lam_neg_in)) || (rc = check_fields(lam_pos_out, lam_neg_out, pos, neg)))
@@ -432,6 +436,7 @@ int pic_adjoint_forward(const pic_grid *g, void *pos0, void *neg0, void *pos1, v
                         const double *xs, const double *ys, const int64_t *track_offsets, void *dens_keep,
                         uint32_t *counts, double *tally, void *ckpt_pos, void *ckpt_neg, int64_t ckpt_every,
                         int64_t state_stride, void *workspace, int64_t workspace_bytes, uintptr_t stream) {
+    NvtxRange nvtx_range("pic_adjoint_forward");
     int rc = check_grid(g);
     if (rc) return rc;
     if ((rc = check_fields(pos0, neg0, pos1, neg1)) || (rc = check_fields(ckpt_pos, ckpt_neg, ckpt_pos, ckpt_neg)))
@@ -485,6 +490,7 @@ int pic_adjoint_backward(const pic_grid *g, const void *ckpt_pos, const void *ck
                          void *states_pos, void *states_neg, void *lam_pos0, void *lam_neg0, void *lam_pos1,
                          void *lam_neg1, double *grad, void *workspace,
                          int64_t workspace_bytes, void *adj_workspace, int64_t adj_workspace_bytes, uintptr_t stream) {
+    NvtxRange nvtx_range("pic_adjoint_backward");
     int rc = check_grid(g);
     if (rc) return rc;
     if ((rc = check_fields(ckpt_pos, ckpt_neg, states_pos, states_neg)) ||
@@ -589,6 +595,7 @@ int pic_revolve_forward(const pic_grid *g, void *pos0, void *neg0, void *pos1, v
                         const double *xs, const double *ys, const int64_t *track_offsets, void *dens,
                         uint32_t *counts, double *tally, void *slots_pos, void *slots_neg, int64_t state_stride,
                         int64_t n_slots, void *workspace, int64_t workspace_bytes, uintptr_t stream) {
+    NvtxRange nvtx_range("pic_revolve_forward");
     int rc = check_revolve(g, slots_pos, slots_neg, state_stride, n_slots, n_steps, xs, ys, track_offsets, dens);
     if (rc) return rc;
     if ((rc = check_fields(pos0, neg0, pos1, neg1))) return rc;
@@ -605,6 +612,7 @@ int pic_revolve_backward(const pic_grid *g, void *slots_pos, void *slots_neg, in
                          void *lam_pos0, void *lam_neg0, void *lam_pos1, void *lam_neg1, double *grad,
                          void *workspace, int64_t workspace_bytes, void *adj_workspace, int64_t adj_workspace_bytes,
                          uintptr_t stream) {
+    NvtxRange nvtx_range("pic_revolve_backward");
     int rc = check_revolve(g, slots_pos, slots_neg, state_stride, n_slots, n_steps, xs, ys, track_offsets, dens);
     if (rc) return rc;
     if ((rc = check_fields(work_pos0, work_neg0, work_pos1, work_neg1)) ||
@@ -626,6 +634,7 @@ int pic_run_segment(const pic_grid *g, void *pos0, void *neg0, void *pos1, void 
                     int64_t n_steps, const double *xs, const double *ys, const int64_t *track_offsets,
                     void *dens0, void *dens1, int64_t dens_parity, uint32_t *counts, double *tally,
                     void *workspace, int64_t workspace_bytes, uintptr_t stream) {
+    NvtxRange nvtx_range("pic_run_segment");
     int rc = check_segment(g, pos0, neg0, pos1, neg1, n_steps, xs, ys, track_offsets, dens0, dens1, counts, tally,
                            workspace, workspace_bytes);
     if (rc) return rc;
@@ -637,6 +646,7 @@ int pic_graph_create(const pic_grid *g, void *pos0, void *neg0, void *pos1, void
                      int64_t n_steps, const double *xs, const double *ys, const int64_t *track_offsets,
                      void *dens0, void *dens1, int64_t dens_parity, uint32_t *counts, double *tally,
                      void *workspace, int64_t workspace_bytes, uintptr_t stream, uintptr_t *graph_out) {
+    NvtxRange nvtx_range("pic_graph_create");
     if (!graph_out) return set_error(PIC_E_INVALID, "graph_out is null");
     *graph_out = 0;
     int rc = check_segment(g, pos0, neg0, pos1, neg1, n_steps, xs, ys, track_offsets, dens0, dens1, counts, tally,
@@ -673,6 +683,7 @@ int pic_graph_create(const pic_grid *g, void *pos0, void *neg0, void *pos1, void
 }
 
 int pic_capture_begin(uintptr_t stream) {
+    NvtxRange nvtx_range("pic_capture_begin");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     if (st == nullptr || st == cudaStreamLegacy || st == cudaStreamPerThread)
         return set_error(PIC_E_INVALID, "capture needs a stream created by the caller (not the default stream)");
@@ -681,6 +692,7 @@ int pic_capture_begin(uintptr_t stream) {
 }
 
 int pic_capture_end(uintptr_t stream, uintptr_t *graph_out) {
+    NvtxRange nvtx_range("pic_capture_end");
     if (!graph_out) return set_error(PIC_E_INVALID, "graph_out is null");
     *graph_out = 0;
     cudaGraph_t graph = nullptr;
@@ -703,6 +715,7 @@ int pic_batched_workspace_bytes(int32_t n_blocks, int32_t n_cfgs, int64_t *bytes
 }
 
 int pic_batched_segment(const pic_batch_launch *launch, uintptr_t stream) {
+    NvtxRange nvtx_range("pic_batched_segment");
     int rc = check_batch(launch);
     if (rc) return rc;
     return batched_loop(*launch, reinterpret_cast<cudaStream_t>(stream));
@@ -710,6 +723,7 @@ int pic_batched_segment(const pic_batch_launch *launch, uintptr_t stream) {
 
 int pic_batched_persistent(const pic_batch_launch *launch, const int64_t *step_task_off_dev,
                            const int64_t *step_tracks_dev, uintptr_t stream) {
+    NvtxRange nvtx_range("pic_batched_persistent");
     int rc = check_batch(launch);  // validates the host copies of the step tables
     if (rc) return rc;
     if (!step_task_off_dev || !step_tracks_dev) return set_error(PIC_E_INVALID, "device step tables are null");
@@ -723,6 +737,7 @@ int pic_batched_status(const pic_batch_launch *launch, uintptr_t stream, int32_t
 }
 
 int pic_batched_graph_create(const pic_batch_launch *launch, uintptr_t stream, uintptr_t *graph_out) {
+    NvtxRange nvtx_range("pic_batched_graph_create");
     if (!graph_out) return set_error(PIC_E_INVALID, "graph_out is null");
     *graph_out = 0;
     int rc = check_batch(launch);
@@ -757,6 +772,7 @@ int pic_batched_graph_create(const pic_batch_launch *launch, uintptr_t stream, u
 }
 
 int pic_graph_launch(uintptr_t graph, uintptr_t stream) {
+    NvtxRange nvtx_range("pic_graph_launch");
     if (!graph) return set_error(PIC_E_INVALID, "graph handle is null");
     cudaError_t e = cudaGraphLaunch(reinterpret_cast<cudaGraphExec_t>(graph), reinterpret_cast<cudaStream_t>(stream));
     return e == cudaSuccess ? PIC_OK : set_cuda_error("cudaGraphLaunch", e);

@@ -7,6 +7,8 @@
 
 #include <string>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/pic_gb300.h"
 
 namespace pic {
@@ -112,6 +114,17 @@ __host__ __device__ inline bool scored_column(const ScoreTest &t, int64_t i, int
 // Row pitch of the 2D density: no_xy rounded up to 4 elements, so every row
 // starts 16-byte aligned and a row segment can be fetched by a bulk copy.
 inline int64_t dens_pitch(int64_t no_xy) { return (no_xy + 3) / 4 * 4; }
+
+// A named NVTX range over an entry point's host-side work (header-only NVTX:
+// a no-op unless a profiler is attached), so that a kernel launch list taken
+// with ncu --nvtx splits by phase: segments, graph replays, batched steps,
+// gradient passes.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 int set_error(int code, const std::string &msg);
 int set_cuda_error(const char *what, cudaError_t e);

@@ -11,6 +11,7 @@ stream; every kernel is the library's.
 from __future__ import annotations
 
 import ctypes
+from contextlib import contextmanager
 
 import numpy as np
 
@@ -20,6 +21,20 @@ from .constants import recombination_alpha
 _DTYPES = {"float32": N.PIC_F32, "float64": N.PIC_F64}
 _VARIANTS = {"auto": N.PIC_VARIANT_AUTO, "flat": N.PIC_VARIANT_FLAT, "stream": N.PIC_VARIANT_STREAM}
 SHAPE_FIELDS = ("variant", "tile_rows", "planes_per_item", "stages", "consumer_warps", "ctas_per_sm", "steps_per_launch")
+
+
+@contextmanager
+def nvtx_range(name: str):
+    """An NVTX range over the enclosed host work (the library's entry points
+    open their own ranges inside it): a launch list taken with ncu --nvtx then
+    splits by phase. A no-op unless a profiler is attached."""
+    import torch
+
+    torch.cuda.nvtx.range_push(name)
+    try:
+        yield
+    finally:
+        torch.cuda.nvtx.range_pop()
 
 
 def apply_shape(g: N.PicGrid, shape: dict | None) -> N.PicGrid:

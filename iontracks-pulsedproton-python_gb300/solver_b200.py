@@ -33,7 +33,7 @@ from typing import Optional
 
 import numpy as np
 
-from .engine import ChamberEngine
+from .engine import ChamberEngine, nvtx_range
 from .feeder import TrackFeeder
 from .pulses import TrackSampler, build_track_schedule
 from .state import Diagnostics, collection_efficiency
@@ -144,13 +144,14 @@ def run_simulation_b200(
                 # draw the next chunk's tracks while the device runs this one
                 pending = submit(next_feed) if next_feed < len(feeds) else None
             seg = offsets[c0 : c1 + 1] - offsets[c0]
-            if use_graphs:
-                # the same chunk of every pulse (or of every idle stretch) has
-                # the same offsets; the parities complete the key
-                key = (with_tracks, c0 if with_tracks else -1, c1 - c0, eng.parity, eng.step_index & 1)
-                eng.run_segment_graphed(key, seg, track_base=int(offsets[c0]))
-            else:
-                eng.run_segment(seg, track_base=int(offsets[c0]))
+            with nvtx_range("pulse steps" if with_tracks else "idle steps"):
+                if use_graphs:
+                    # the same chunk of every pulse (or of every idle stretch)
+                    # has the same offsets; the parities complete the key
+                    key = (with_tracks, c0 if with_tracks else -1, c1 - c0, eng.parity, eng.step_index & 1)
+                    eng.run_segment_graphed(key, seg, track_base=int(offsets[c0]))
+                else:
+                    eng.run_segment(seg, track_base=int(offsets[c0]))
             steps_done = s0 + c1
             if progress and (steps_done // report_every) != ((s0 + c0) // report_every):
                 print(f"  step {steps_done}/{total}")
