@@ -162,6 +162,18 @@ def _interior(cfg):
     return (cfg.no_xy - 2) ** 2 * (cfg.no_z_with_buffer - 2)
 
 
+def _workload_config(cfg, desc, timed_tracks, world):
+    """The line's ``config``: the same dict on both arms' lines."""
+    read_mb = 2 * int(cfg.no_xy) ** 2 * ((int(cfg.no_z_with_buffer) + 7) // 8 * 8) * 4 / 1e6
+    l2_note = (f"each step reads {read_mb:.0f} MB of float32 fields, more than the 129 MB L2: inputs larger than "
+               "L2, no flush needed" if read_mb > 129 else
+               f"each step reads {read_mb:.0f} MB of float32 fields, less than the 129 MB L2: L2-resident between "
+               "steps (no flush; an upper bound, not an HBM measurement)")
+    return {"workload": desc, "grid": [int(cfg.no_xy), int(cfg.no_xy), int(cfg.no_z_with_buffer)],
+            "interior_voxels": int(_interior(cfg)), "tracks_in_timed_steps": int(timed_tracks), "l2": l2_note,
+            "parallelism": f"replicas x{world}"}
+
+
 def cpu_sample(cfg, steps=3, warmup=2, threads=None):
     """FP64 oracle (the reference algorithm in C/OpenMP, batched deposition)
     on pulse steps of the workload, on all host cores. The first ``warmup``
@@ -186,11 +198,12 @@ def run_reference(args):
     steps = max(1, min(args.steps, args.ref_max_steps))
     warmup = max(1, min(args.warmup, 5))
     v, cores, wall = cpu_sample(cfg, steps=steps, warmup=warmup)
+    sched = _pkg().build_track_schedule(cfg, np.random.default_rng(cfg.seed))
     line = {
         "impl": "reference", "metric": "interior voxel-steps/s", "value": v, "unit": "voxel-steps/s",
         "n_gpus": world, "steps": steps, "warmup": warmup, "ms_per_step": wall / steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": desc},
+        "config": _workload_config(cfg, desc, sched[warmup:warmup + steps].sum(), world),
         "cpu_baseline": {"value": v, "unit": "voxel-steps/s", "cores": cores, "kind": "port",
                          "sample": f"{steps} pulse steps of the workload (deposition + sweep) after {warmup} untimed, "
                                    f"FP64 oracle (C/OpenMP restatement of the reference kernels), {wall:.1f} s timed"},
@@ -200,21 +213,25 @@ def run_reference(args):
     return 0
 
 
-def run_sweep(args):
-    """The 64-configuration saturation sweep: one batched run against the same
-    64 plain solves run one after another on the same GPU (both end to end:
-    host track sampling, uploads, all steps, read-back)."""
-    import torch
-    import torch.distributed as dist
+def _oracle_sweep_fixture():
+    """Per-configuration float64 oracle results of the 64-grid sweep
+    (tests/golden/oracle_sweep64.json, made by tests/golden/make_oracle_fixtures.py),
+    or None when the file is absent."""
+    p = ROOT / "tests" / "golden" / "oracle_sweep64.json"
+    return json.loads(p.read_text())["configs"] if p.exists() else None
 
-    world, rank = _dist()
-    if world > 1:
-        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        dist.init_process_group("nccl")
+
+def sweep_measure(n_configs=64, batched_only=False, rank=0, world=1):
+    """The 64-configuration saturation sweep: one batched run against the same
+    configurations solved one after another with the plain solver on the
+    same GPU, both end to end (host track sampling, uploads, all steps,
+    read-back). Returns this rank's numbers (its share of the sweep)."""
+    import torch
+
     pkg = _pkg()
-    replicas = importlib.import_module(PACKAGE + ".replicas")
-    every = pkg.saturation_sweep_configs()[: max(1, args.sweep_configs)]
-    cfgs = every[rank::world]  # the sweep's configurations shared out over the GPUs
+    every = pkg.saturation_sweep_configs()[: max(1, n_configs)]
+    idx = list(range(len(every)))[rank::world]  # the sweep's configurations shared out over the GPUs
+    cfgs = [every[i] for i in idx]
     vox = sum(_interior(c) * int(c.total_time_steps) for c in cfgs)
     # warm-up: load the kernels, pay first-use costs outside the timing
     pkg.run_batched_b200(cfgs[:2])
@@ -224,55 +241,84 @@ def run_sweep(args):
     batch = pkg.run_batched_b200(cfgs)
     torch.cuda.synchronize()
     t_batch = time.perf_counter() - t0
-    if args.batched_only:
-        plain, t_plain, dks = None, None, None
-    else:
+    plain, t_plain, dks = None, None, None
+    if not batched_only:
         t0 = time.perf_counter()
         plain = [pkg.run_simulation_b200(c, progress=False, return_fields=False) for c in cfgs]
         torch.cuda.synchronize()
         t_plain = time.perf_counter() - t0
         dks = max(abs(b.ks - p.ks) for b, p in zip(batch, plain))
-    value = replicas.whole_job_rate(vox, t_batch)
-    t_batch = replicas.max_over_ranks(t_batch)
-    vox = replicas.sum_over_ranks(vox)
+    fx = _oracle_sweep_fixture()
+    dks_oracle = None
+    if fx is not None and len(fx) == 64:
+        dks_oracle = max(abs(b.ks - fx[i]["ks"]) for b, i in zip(batch, idx))
+    return {"configs": len(cfgs), "interior_voxel_steps": vox, "batched_s": t_batch, "sequential_plain_s": t_plain,
+            "speedup_vs_sequential": None if t_plain is None else t_plain / t_batch,
+            "max_abs_dks_batched_vs_plain": dks, "max_abs_dks_batched_vs_fp64_oracle": dks_oracle,
+            "n_total": len(every)}
+
+
+def run_sweep(args):
+    """--workload saturation_sweep: the sweep alone, shared out over ranks."""
+    import torch
+    import torch.distributed as dist
+
+    world, rank = _dist()
+    if world > 1:
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    replicas = importlib.import_module(PACKAGE + ".replicas")
+    m = sweep_measure(args.sweep_configs, args.batched_only, rank, world)
+    value = replicas.whole_job_rate(m["interior_voxel_steps"], m["batched_s"])
+    t_batch = replicas.max_over_ranks(m["batched_s"])
+    vox = replicas.sum_over_ranks(m["interior_voxel_steps"])
+    t_plain, dks = m["sequential_plain_s"], m["max_abs_dks_batched_vs_plain"]
     if t_plain is not None:
         t_plain = replicas.max_over_ranks(t_plain)
         dks = replicas.max_over_ranks(dks)
+    dko = m["max_abs_dks_batched_vs_fp64_oracle"]
+    if dko is not None:
+        dko = replicas.max_over_ranks(dko)
     if world > 1:
         dist.destroy_process_group()
     if rank == 0:
         line = {
             "metric": "interior voxel-steps/s, 64-config saturation sweep", "value": value,
-            "unit": "voxel-steps/s", "n_gpus": world, "steps": int(max(c.total_time_steps for c in every)),
+            "unit": "voxel-steps/s", "n_gpus": world, "steps": int(max(c.total_time_steps for c in
+                                                                        _pkg().saturation_sweep_configs())),
             "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"saturation sweep: {len(every)} of 64 configs, 25-400 V log-spaced, gaps "
-                                   "0.1/0.2/0.3 cm, 1-100 Gy/s, 100-1000 us pulses, 5/10 um voxels, "
-                                   "r 0.008-0.03 cm, seeds 1-64", "interior_voxel_steps": vox},
+            "config": {"workload": SWEEP_DESC.format(n=m["n_total"]), "interior_voxel_steps": vox},
             "batched_s": t_batch, "sequential_plain_s": t_plain,
             "speedup_vs_sequential": None if t_plain is None else t_plain / t_batch,
-            "max_abs_dks_batched_vs_plain": dks,
+            "max_abs_dks_batched_vs_plain": dks, "max_abs_dks_batched_vs_fp64_oracle": dko,
         }
         print(json.dumps(line), flush=True)
     return 0
 
 
-def run_adjoint(args):
+SWEEP_DESC = ("saturation sweep: {n} of 64 configs, 25-400 V log-spaced, gaps 0.1/0.2/0.3 cm, 1-100 Gy/s, "
+              "100-1000 us pulses, 5/10 um voxels, r 0.008-0.03 cm, seeds 1-64")
+
+
+ADJOINT_CFG = dict(BEAM, grid_size_um=10.0, sampled_radius_cm=0.02, seed=1)
+
+
+def adjoint_measure(warmup=3, reps=3):
     """A full gradient dk_s/d(alpha, mu+, mu-, D+, D-, V) (checkpointed
     forward + reverse sweep, checkpoints every 64 steps, float32) against one
     plain forward solve of the same chamber, both end to end through the
-    package API, on the 10 um, r = 0.02 cm column at 300 V."""
+    package API, on the 10 um, r = 0.02 cm column at 300 V (medians)."""
     import torch
 
-    world, rank = _dist()
     pkg = _pkg()
     adj = importlib.import_module(PACKAGE + ".adjoint")
-    cfg = pkg.SimulationConfig(**BEAM, grid_size_um=10.0, sampled_radius_cm=0.02, seed=1)
-    for _ in range(max(1, args.warmup)):
+    cfg = pkg.SimulationConfig(**ADJOINT_CFG)
+    for _ in range(max(1, warmup)):
         pkg.run_simulation_b200(cfg, progress=False, return_fields=False)
         adj.ks_and_gradient(cfg, checkpoint_every=64)
     plain, full, parts = [], [], []
-    for _ in range(max(1, args.steps)):
+    for _ in range(max(1, reps)):
         torch.cuda.synchronize()
         t = time.perf_counter()
         res = pkg.run_simulation_b200(cfg, progress=False, return_fields=False)
@@ -284,19 +330,28 @@ def run_adjoint(args):
         full.append(time.perf_counter() - t)
         parts.append(tm)
     p, f = statistics.median(plain), statistics.median(full)
-    if rank == 0:
-        print(json.dumps({
-            "metric": "full adjoint gradient wall time / one plain forward solve", "value": f / p, "unit": "x",
-            "n_gpus": world, "steps": len(full), "warmup": args.warmup, "ms_per_step": None,
-            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"10 um column, r 0.02 cm, {cfg.no_xy}x{cfg.no_xy}x{cfg.no_z_with_buffer}, "
-                                   f"{cfg.total_time_steps} steps, 300 V / 0.2 cm, 8.91 Gy/s, seed 1; "
-                                   "checkpoints every 64 steps", "parameters": list(adj.PARAMS)},
-            "plain_forward_s": p, "adjoint_total_s": f,
+    return {"ratio": f / p, "plain_forward_s": p, "adjoint_total_s": f,
             "adjoint_forward_s": statistics.median(t["forward_s"] for t in parts),
             "adjoint_backward_s": statistics.median(t["backward_s"] for t in parts),
-            "ks": ks, "ks_plain": res.ks, "dks_dtheta": list(grad),
-        }), flush=True)
+            "ks": ks, "ks_plain": res.ks, "dks_dtheta": list(grad), "parameters": list(adj.PARAMS),
+            "workload": f"10 um column, r 0.02 cm, {cfg.no_xy}x{cfg.no_xy}x{cfg.no_z_with_buffer}, "
+                        f"{cfg.total_time_steps} steps, 300 V / 0.2 cm, 8.91 Gy/s, seed 1; checkpoints every 64 "
+                        "steps"}
+
+
+def run_adjoint(args):
+    """--workload adjoint: the gradient-over-forward ratio alone."""
+    world, rank = _dist()
+    m = adjoint_measure(args.warmup, args.steps)
+    if rank == 0:
+        line = {
+            "metric": "full adjoint gradient wall time / one plain forward solve", "value": m["ratio"], "unit": "x",
+            "n_gpus": world, "steps": max(1, args.steps), "warmup": args.warmup, "ms_per_step": None,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": m.pop("workload"), "parameters": m.pop("parameters")},
+        }
+        line.update({k: v for k, v in m.items() if k != "ratio"})
+        print(json.dumps(line), flush=True)
     return 0
 
 
@@ -478,22 +533,28 @@ def run_gb300(args):
                "sample": f"{args.cpu_steps} pulse steps of the same workload after 2 untimed (page first-touch), "
                          f"FP64 oracle, {wall:.1f} s timed"}
 
-    es = 4 if args.dtype == "float32" else 8
-    read_mb = 2 * int(cfg.no_xy) ** 2 * ((int(cfg.no_z_with_buffer) + 7) // 8 * 8) * es / 1e6
-    l2_note = (f"each step reads {read_mb:.0f} MB of fields, more than the 129 MB L2: inputs larger than L2, "
-               "no flush needed" if read_mb > 129 else
-               f"each step reads {read_mb:.0f} MB of fields, less than the 129 MB L2: L2-resident between steps "
-               "(no flush; an upper bound, not an HBM measurement)")
+    # the benchmark spec's other two ratios, on the same line: the 64-grid sweep
+    # (batched vs the same solves one after another) and the configs' gradient
+    # (full adjoint vs one forward solve), each end to end through the
+    # package's API on this GPU
+    sweep = adjoint = None
+    if not args.no_extras:
+        if world == 1:
+            torch.cuda.empty_cache()
+            sweep = sweep_measure()
+            sweep["workload"] = SWEEP_DESC.format(n=sweep.pop("n_total"))
+            adjoint = adjoint_measure(warmup=3, reps=3)
+        else:
+            sweep = adjoint = {"skipped": "measured by the single-GPU run only"}
+
     if rank == 0:
         line = {
             "metric": "interior voxel-steps/s", "value": value, "unit": "voxel-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.dtype == "float32" else "f64",
             "data": "synthetic",
-            "config": {"workload": desc, "grid": [cfg.no_xy, cfg.no_xy, cfg.no_z_with_buffer],
-                       "interior_voxels": vox, "tracks_in_timed_steps": int(counts[args.warmup:].sum()),
-                       "l2": l2_note,
-                       "parallelism": f"replicas x{world}", "launch_shape": resolved},
+            "config": _workload_config(cfg, desc, counts[args.warmup:].sum(), world),
+            "launch_shape": resolved,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                          "kernel": "stream_step_kernel" if resolved["variant"] == "stream" else "step_kernel",
@@ -506,6 +567,8 @@ def run_gb300(args):
             "e2e": e2e,
             "gpu_launches": launches,
             "clocks": clk.summary(),
+            "sweep": sweep,
+            "adjoint": adjoint,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -528,6 +591,8 @@ def main():
     ap.add_argument("--ref-max-steps", dest="ref_max_steps", type=int, default=300,
                     help="--impl reference: at most this many timed steps")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", dest="no_extras", action="store_true",
+                    help="skip the sweep and gradient measurements embedded in the default line")
     ap.add_argument("--batched-only", dest="batched_only", action="store_true",
                     help="saturation_sweep: time the batched run only (profiling)")
     ap.add_argument("--sweep-configs", dest="sweep_configs", type=int, default=64,

@@ -37,6 +37,15 @@ def test_reference_arm_line():
     assert cb["value"] == d["value"] and cb["kind"] == "port" and cb["cores"] >= 1 and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert "workload" in d["config"] and "24x24x206" in d["config"]["workload"]
+    # the same config dict as the GB300 arm's line: the workload, its grid and
+    # the tracks of the timed steps (the GB300 arm builds it with the same helper)
+    c = d["config"]
+    assert c["grid"] == [24, 24, 206] and c["interior_voxels"] == 22 * 22 * 204
+    assert {"tracks_in_timed_steps", "l2", "parallelism"} <= set(c)
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    assert set(c) == set(bench._workload_config(bench._config("column_10um_r008")[1], "x", 0, 1))
 
 
 def test_reference_arm_other_ranks_silent():
