@@ -48,3 +48,17 @@ def run_config(name):
 
 def available(name):
     return (GOLDEN / f"{name}.npz").exists()
+
+
+def oracle_fixture(name):
+    """Whole-run float64 oracle results written by
+    tests/golden/make_oracle_fixtures.py (``oracle_sweep64`` or
+    ``oracle_column_5um_r05``)."""
+    return json.loads((GOLDEN / f"{name}.json").read_text())
+
+
+def histogram_sha256(track_density_xy) -> str:
+    """SHA-256 of a track histogram as uint32 in C order (the fixtures' form)."""
+    import hashlib
+
+    return hashlib.sha256(np.ascontiguousarray(np.asarray(track_density_xy).astype(np.uint32)).tobytes()).hexdigest()

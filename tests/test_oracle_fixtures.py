@@ -1,0 +1,48 @@
+"""The whole-run oracle fixtures (tests/golden/make_oracle_fixtures.py) are
+the oracle's own numbers for the configurations the package builds today
+(CPU): sizes, seeds and track counts match the sweep and plain-at-scale
+definitions, and re-running the oracle on the smallest sweep grids
+reproduces the recorded k_s and track checksums bit for bit."""
+
+import numpy as np
+import pytest
+
+from goldens import histogram_sha256, make_config, oracle_fixture, pkg
+
+
+def test_sweep_fixture_matches_the_sweep_definition():
+    fx = oracle_fixture("oracle_sweep64")["configs"]
+    cfgs = pkg().saturation_sweep_configs()
+    assert len(fx) == len(cfgs) == 64
+    for c, f in zip(cfgs, fx):
+        assert (c.no_xy, c.no_z_with_buffer, c.total_time_steps, c.seed) == (f["no_xy"], f["nzb"],
+                                                                             f["total_time_steps"], f["seed"])
+        assert c.voltage_V == f["voltage_V"] and c.dose_rate_Gy_s == f["dose_rate_Gy_s"]
+        sched = pkg().build_track_schedule(c, np.random.default_rng(c.seed))
+        assert int(sched.sum()) == f["n_tracks"]
+        assert np.isfinite(f["ks"]) and f["ks"] > 1.0 and f["injected_sum"] > f["recombined_sum"] > 0.0
+
+
+def test_plain_at_scale_fixture_matches_its_configurations():
+    runs = oracle_fixture("oracle_column_5um_r05")["runs"]
+    assert len(runs) == 8
+    for name in ("column_5um_r05_d8p91", "column_5um_r05_d89p1"):
+        for seed in (1, 2, 3, 4):
+            f = runs[f"{name}_seed{seed}"]
+            c = make_config(name, seed=seed)
+            assert (c.no_xy, c.no_z_with_buffer, c.total_time_steps) == (208, 406, 3388)
+            assert (f["no_xy"], f["nzb"], f["total_time_steps"], f["seed"]) == (208, 406, 3388, seed)
+            sched = pkg().build_track_schedule(c, np.random.default_rng(seed))
+            assert int(sched.sum()) == f["n_tracks"]
+
+
+@pytest.mark.parametrize("rank", [0, 1])
+def test_oracle_reproduces_the_sweep_fixture(oracle, rank):
+    cfgs = pkg().saturation_sweep_configs()
+    fx = oracle_fixture("oracle_sweep64")["configs"]
+    order = sorted(range(64), key=lambda i: cfgs[i].no_xy ** 2 * cfgs[i].no_z_with_buffer * cfgs[i].total_time_steps)
+    i = order[rank]
+    res = oracle.run(cfgs[i], mode="batched", threads=1, keep_fields=False)
+    assert res["ks"] == fx[i]["ks"]
+    assert histogram_sha256(res["track_density_xy"]) == fx[i]["track_sha256"]
+    assert float(res["recombined"].sum()) == fx[i]["recombined_sum"]
