@@ -167,6 +167,47 @@ def test_batched_sweep_subset_matches_the_oracle(oracle):
         assert abs(got.ks - ref["ks"]) <= KS_ABS
 
 
+def _check_against_sweep_fixture(results, idx, what):
+    from goldens import histogram_sha256, oracle_fixture
+
+    fx = oracle_fixture("oracle_sweep64")["configs"]
+    assert len(fx) == 64
+    bad = []
+    for i, got in zip(idx, results):
+        ref = fx[i]
+        same_tracks = histogram_sha256(got.track_density_xy) == ref["track_sha256"]
+        if np.isnan(ref["ks"]):
+            # the reference's scheme diverges on this configuration (the
+            # oracle's tallies overflow): the float32 run must not report a
+            # finite k_s either
+            ok = same_tracks and not np.isfinite(got.ks)
+        else:
+            ok = (same_tracks and abs(got.ks - ref["ks"]) <= KS_ABS
+                  and abs(got.injected_positive.sum() / ref["injected_sum"] - 1.0) <= 1e-5
+                  and abs(got.recombination.sum() / ref["recombined_sum"] - 1.0) <= 1e-5)
+        if not ok:
+            bad.append((i, got.ks, ref["ks"]))
+    assert not bad, f"{what}: configurations off the float64 oracle: {bad}"
+
+
+@pytest.mark.gpu
+def test_whole_sweep_batched_matches_the_oracle_fixtures():
+    """All 64 configurations of the saturation sweep in one float32 batched run,
+    each against the float64 oracle's run of it (tests/golden/oracle_sweep64.json):
+    identical tracks (histogram checksum), |dk_s| <= 1e-5, total injected and
+    recombined charge within 1e-5 relative."""
+    cfgs = pkg().saturation_sweep_configs()
+    _check_against_sweep_fixture(pkg().run_batched_b200(cfgs), range(64), "batched")
+
+
+@pytest.mark.gpu
+def test_whole_sweep_plain_solves_match_the_oracle_fixtures():
+    """The same 64 configurations through the plain solver, one after another."""
+    cfgs = pkg().saturation_sweep_configs()
+    res = [pkg().run_simulation_b200(c, progress=False, return_fields=False) for c in cfgs]
+    _check_against_sweep_fixture(res, range(64), "plain")
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("dtype", ["float32", "float64"])
 def test_persistent_launch_matches_per_step_launches(dtype):
@@ -207,3 +248,88 @@ def test_single_grid_phases_match_batched_launches(dtype):
             peak = max(np.abs(x.positive_array).max(), 1e-300)
             np.testing.assert_allclose(y.positive_array, x.positive_array, rtol=0, atol=tol * peak)
             np.testing.assert_allclose(y.negative_array, x.negative_array, rtol=0, atol=tol * peak)
+
+
+def _stream_mod():
+    import importlib
+
+    return importlib.import_module(pkg().__name__ + ".batched")
+
+
+def test_stream_items_cover_every_interior_voxel_once():
+    """The streaming batched step's item table (CPU): for every phase of the
+    64-grid sweep, each active grid's interior rows x planes are covered
+    exactly once, a grid's items are consecutive, tiles fit the consumer
+    threads and a ring stage, and about six items per SM come out."""
+    B = _stream_mod()
+    cfgs = pkg().saturation_sweep_configs()
+    shapes = [(int(c.no_xy), int(c.no_z_with_buffer), (int(c.no_z_with_buffer) + 7) // 8 * 8) for c in cfgs]
+    totals = [int(c.total_time_steps) for c in cfgs]
+    for sms in (152, 7):
+        for s0, s1, active in B._phases(totals):
+            items, tiles = B._stream_items(shapes, active, sms)
+            assert items.dtype == np.int32 and items.shape[1] == 4
+            grids_seen = []
+            for c in items[:, 0]:
+                if not grids_seen or grids_seen[-1] != c:
+                    assert c not in grids_seen, "items of a grid are not consecutive"
+                    grids_seen.append(int(c))
+            assert sorted(grids_seen) == sorted(active)
+            for c in active:
+                n, nzb, kp = shapes[c]
+                tj = int(tiles[c])
+                assert 1 <= tj <= n - 2 and tj * (kp // 4) <= B.STREAM_IPT * 32 * B.STREAM_WARPS
+                assert B._stage_floats(tj, kp) * 4 <= B.STREAM_STAGE_BYTES
+                cover = np.zeros((n, n), dtype=np.int32)  # (plane, row)
+                for _, j0, i0, i1 in items[items[:, 0] == c]:
+                    assert 1 <= j0 <= n - 2 and 1 <= i0 < i1 <= n - 1
+                    cover[i0:i1, j0:min(j0 + tj, n - 1)] += 1
+                assert (cover[1:-1, 1:-1] == 1).all() and cover[0].sum() == 0 and cover[-1].sum() == 0
+                assert cover[:, 0].sum() == 0 and cover[:, -1].sum() == 0
+        # the heavy first phase: a few items per SM
+        items, _ = B._stream_items(shapes, list(range(64)), sms)
+        assert len(items) >= 2 * sms
+
+
+def test_stream_variant_arguments_are_checked_before_device_work():
+    B = _stream_mod()
+    cfg = make_config("fast")
+    with pytest.raises(ValueError, match="variant"):
+        B.run_batched_b200([cfg], variant="tiled")
+    with pytest.raises(ValueError, match="float32"):
+        B.run_batched_b200([cfg], variant="stream", dtype="float64")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("solo", [0, 2])
+def test_stream_batched_step_matches_the_flat_one(solo):
+    """The streaming batched step (items of every grid from a device-wide
+    queue, planes staged in a shared-memory ring) against the flat batched
+    step on the mixed batch (both walls, odd no_xy, the full-grid scoring
+    region, two species): identical tracks, k_s and tallies within 1e-5,
+    fields within 1e-5 of their peak; chunks of 7 global steps, with and
+    without the single-grid tail phases."""
+    cfgs = _mixed_batch()
+    a = pkg().run_batched_b200(cfgs, chunk_steps=7, solo_grids=solo, variant="flat", return_fields=True)
+    b = pkg().run_batched_b200(cfgs, chunk_steps=7, solo_grids=solo, variant="stream", return_fields=True)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x.track_density_xy, y.track_density_xy)
+        assert abs(x.ks - y.ks) <= KS_ABS
+        np.testing.assert_allclose(y.recombination, x.recombination, rtol=0,
+                                   atol=1e-5 * max(np.abs(x.recombination).max(), 1e-300))
+        np.testing.assert_allclose(y.injected_positive, x.injected_positive, rtol=1e-5, atol=0)
+        peak = max(np.abs(x.positive_array).max(), 1e-300)
+        np.testing.assert_allclose(y.positive_array, x.positive_array, rtol=0, atol=1e-5 * peak)
+        np.testing.assert_allclose(y.negative_array, x.negative_array, rtol=0, atol=1e-5 * peak)
+
+
+@pytest.mark.gpu
+def test_stream_batched_matches_the_oracle_on_sweep_grids(oracle):
+    """Eight sweep configurations through the streaming batched step against
+    the float64 oracle, with the streaming step forced on every phase."""
+    cfgs = [c for c in pkg().saturation_sweep_configs() if c.no_xy ** 2 * c.no_z_with_buffer < 1.5e6][:8]
+    batch = pkg().run_batched_b200(cfgs, variant="stream", solo_grids=0)
+    for cfg, got in zip(cfgs, batch):
+        ref = oracle.run(cfg, mode="batched", threads=8, keep_fields=False)
+        np.testing.assert_array_equal(got.track_density_xy, ref["track_density_xy"])
+        assert abs(got.ks - ref["ks"]) <= KS_ABS

@@ -20,7 +20,20 @@ def test_sweep_fixture_matches_the_sweep_definition():
         assert c.voltage_V == f["voltage_V"] and c.dose_rate_Gy_s == f["dose_rate_Gy_s"]
         sched = pkg().build_track_schedule(c, np.random.default_rng(c.seed))
         assert int(sched.sum()) == f["n_tracks"]
-        assert np.isfinite(f["ks"]) and f["ks"] > 1.0 and f["injected_sum"] > f["recombined_sum"] > 0.0
+        if np.isnan(f["ks"]):
+            # the reference's explicit scheme diverges on this configuration
+            # (carriers go negative after the pulse and the recombination term
+            # grows without bound): the oracle's run ends in non-finite tallies
+            assert not np.isfinite(f["recombined_sum"])
+            continue
+        assert f["ks"] > 1.0 and f["injected_sum"] > f["recombined_sum"] > 0.0
+
+
+def test_exactly_one_sweep_configuration_diverges():
+    """Configuration 27 (seed 28: 82 V over 0.3 cm at 50.5 Gy/s, 10 um voxels,
+    dt 1.74 us) is the one the reference's scheme does not survive."""
+    fx = oracle_fixture("oracle_sweep64")["configs"]
+    assert [i for i, f in enumerate(fx) if np.isnan(f["ks"])] == [27]
 
 
 def test_plain_at_scale_fixture_matches_its_configurations():
