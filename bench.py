@@ -234,7 +234,7 @@ def _max_abs_diff(a, b):
     return worst
 
 
-def sweep_measure(n_configs=64, batched_only=False, rank=0, world=1):
+def sweep_measure(n_configs=64, batched_only=False, rank=0, world=1, variant="auto"):
     """The 64-configuration saturation sweep: one batched run against the same
     configurations solved one after another with the plain solver on the
     same GPU, both end to end (host track sampling, uploads, all steps,
@@ -247,11 +247,11 @@ def sweep_measure(n_configs=64, batched_only=False, rank=0, world=1):
     cfgs = [every[i] for i in idx]
     vox = sum(_interior(c) * int(c.total_time_steps) for c in cfgs)
     # warm-up: load the kernels, pay first-use costs outside the timing
-    pkg.run_batched_b200(cfgs[:2])
+    pkg.run_batched_b200(cfgs[:2], variant=variant)
     pkg.run_simulation_b200(cfgs[0], progress=False, return_fields=False)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    batch = pkg.run_batched_b200(cfgs)
+    batch = pkg.run_batched_b200(cfgs, variant=variant)
     torch.cuda.synchronize()
     t_batch = time.perf_counter() - t0
     plain, t_plain, dks = None, None, None
@@ -281,7 +281,7 @@ def run_sweep(args):
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
     replicas = importlib.import_module(PACKAGE + ".replicas")
-    m = sweep_measure(args.sweep_configs, args.batched_only, rank, world)
+    m = sweep_measure(args.sweep_configs, args.batched_only, rank, world, args.sweep_variant)
     value = replicas.whole_job_rate(m["interior_voxel_steps"], m["batched_s"])
     t_batch = replicas.max_over_ranks(m["batched_s"])
     vox = replicas.sum_over_ranks(m["interior_voxel_steps"])
@@ -428,6 +428,43 @@ def run_adjoint_full(args):
             "full_run": {"steps": full, "slots": plan["slots"], "recompute_steps": rec_full,
                          "projected_s": proj, "projected_vs_forward": proj / (full * t_step)},
             "ks": ks, "dks_dtheta": list(grad),
+        }), flush=True)
+    return 0
+
+
+def run_full_electrode_run(args):
+    """The whole 10-pulse run of the 5 um full electrode (seed 1, 985 801
+    steps, 97 % of them without tracks) through run_simulation_b200, once,
+    end to end: its k_s and tallies, the wall time and the mean time per
+    step over the run, with the pulse and idle step counts beside them."""
+    import torch
+
+    world, rank = _dist()
+    pkg = _pkg()
+    desc, cfg = _config("full_electrode_5um")
+    total = int(cfg.total_time_steps)
+    pulse = int(cfg.pulse_time_steps) * int(cfg.n_pulses)
+    steps = total if args.run_steps <= 0 else min(total, int(args.run_steps))
+    # warm-up: load the library, resolve the launch shape
+    pkg.run_simulation_b200(cfg, progress=False, return_fields=False, max_steps=8)
+    torch.cuda.synchronize()
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        t0 = time.perf_counter()
+        res = pkg.run_simulation_b200(cfg, progress=False, return_fields=False,
+                                      max_steps=None if steps == total else steps)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    vox = _interior(cfg)
+    if rank == 0:
+        print(json.dumps({
+            "metric": "interior voxel-steps/s, whole 10-pulse run", "value": vox * steps / wall,
+            "unit": "voxel-steps/s", "n_gpus": world, "steps": steps, "warmup": 1,
+            "ms_per_step": 1e3 * wall / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": _workload_config(cfg, desc + "; the whole run", 0, world),
+            "ks": res.ks, "wall_s": wall, "total_steps": total, "pulse_steps": pulse, "idle_steps": total - pulse,
+            "injected": float(res.injected_positive.sum()), "recombined": float(res.recombination.sum()),
+            "tracks": int(res.track_density_xy.sum()), "clocks": clk.summary(),
         }), flush=True)
     return 0
 
@@ -595,7 +632,10 @@ def main():
     ap.add_argument("--steps", type=int, default=600)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["saturation_sweep", "adjoint", "adjoint_full_electrode"], default="full_electrode_5um")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["saturation_sweep", "adjoint", "adjoint_full_electrode",
+                                                               "full_electrode_run"], default="full_electrode_5um")
+    ap.add_argument("--run-steps", dest="run_steps", type=int, default=0,
+                    help="full_electrode_run: stop after this many steps (0: the whole run)")
     ap.add_argument("--dtype", choices=["float32", "float64"], default="float32")
     ap.add_argument("--e2e-steps", type=int, default=0,
                     help="steps of the end-to-end run (0: the whole first pulse)")
@@ -608,6 +648,8 @@ def main():
                     help="skip the sweep and gradient measurements embedded in the default line")
     ap.add_argument("--batched-only", dest="batched_only", action="store_true",
                     help="saturation_sweep: time the batched run only (profiling)")
+    ap.add_argument("--sweep-variant", dest="sweep_variant", choices=["auto", "flat", "stream"], default="auto",
+                    help="saturation_sweep: the batched step kernel (run_batched_b200's variant)")
     ap.add_argument("--sweep-configs", dest="sweep_configs", type=int, default=64,
                     help="saturation_sweep: run the first N of the 64 configurations (profiling-size cases)")
     ap.add_argument("--adjoint-steps", dest="adjoint_steps", type=int, default=1000,
@@ -632,6 +674,8 @@ def main():
         return run_sweep(args)
     if args.workload == "adjoint":
         return run_adjoint(args)
+    if args.workload == "full_electrode_run":
+        return run_full_electrode_run(args)
     if args.workload == "adjoint_full_electrode":
         return run_adjoint_full(args)
     return run_gb300(args)

@@ -479,6 +479,53 @@ int pic_batched_persistent(const pic_batch_launch *launch, const int64_t *step_t
                            const int64_t *step_tracks_dev, uintptr_t stream);
 int pic_batched_status(const pic_batch_launch *launch, uintptr_t stream, int32_t *status);
 
+/*
+ * The streaming batched step: the same global steps as pic_batched_segment,
+ * with the fused step of every active grid run by the streaming kernel (whole
+ * (row-tile x k) planes staged in a shared-memory ring by bulk asynchronous
+ * copies) over a table of work items from all grids, which the CTAs take from
+ * a device-wide queue. float32 batches only. Replaces, like
+ * pic_batched_segment, running the reference's driver once per configuration
+ * (solver_numba_parallel.py:526-723) for a parameter sweep.
+ *
+ * An item is four int32: grid c, the first interior row cj_lo of its tile
+ * (rows cj_lo .. min(cj_lo + tile_rows[c], no_xy - 1) - 1), and its interior
+ * planes [ci_lo, ci_hi); every interior row and plane of every active grid
+ * must be covered exactly once, and the items of a grid must be consecutive
+ * in the table (grids without items are not stepped). tile_rows[c] x
+ * kpitch/4 must be <= 3 x 32 x consumer_warps.
+ *
+ * pic_batched_stream_prepare validates the host tables (cfgs_host is the host
+ * copy of launch->cfgs), uploads them into the workspace
+ * (pic_batched_stream_workspace_bytes, 256-byte aligned; clears its counters)
+ * and fills *out, the launch shape the segment calls take. It waits for the
+ * upload, so the host tables may be released when it returns. Call it again
+ * whenever the item table changes (a grid finished).
+ * pic_batched_stream_segment runs global steps [first_step, first_step +
+ * n_steps) of `launch` (its task tables and buffers; its flat work table and
+ * workspace are not used) with the prepared tables.
+ * pic_batched_stream_status reads the workspace's status word: 0, 1-3 when a
+ * bounded wait of the copy ring ran out, 7 when an item was refused on the
+ * device; with reset != 0 a non-zero word is cleared together with the queue
+ * and grid counters the aborted step left behind.
+ */
+typedef struct pic_batch_stream {
+    int32_t n_cfgs, n_items;
+    int32_t consumer_warps; /* compute warps per CTA (1 .. 15)               */
+    int32_t stages;         /* ring stages that fit the largest stage        */
+    int32_t stage_floats;   /* floats of one stage (the largest grid's)      */
+    int32_t ipt;            /* k-vectors per consumer thread (1 .. 3)        */
+    void *workspace;
+    int64_t workspace_bytes;
+} pic_batch_stream;
+
+int pic_batched_stream_workspace_bytes(int32_t n_cfgs, int32_t n_items, int32_t consumer_warps, int64_t *bytes);
+int pic_batched_stream_prepare(const pic_batch_cfg *cfgs_host, int32_t n_cfgs, const int32_t *items_host,
+                               int32_t n_items, const int32_t *tile_rows_host, int32_t consumer_warps,
+                               void *workspace, int64_t workspace_bytes, uintptr_t stream, pic_batch_stream *out);
+int pic_batched_stream_segment(const pic_batch_launch *launch, const pic_batch_stream *bs, uintptr_t stream);
+int pic_batched_stream_status(const pic_batch_stream *bs, int32_t reset, uintptr_t stream, int32_t *status);
+
 #ifdef __cplusplus
 }
 #endif

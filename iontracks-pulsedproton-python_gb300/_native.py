@@ -183,6 +183,18 @@ EXPORTS = {
     "pic_batched_workspace_bytes": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]),
     "pic_batched_segment": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "pic_batched_graph_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "pic_batched_stream_workspace_bytes": (
+        ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]
+    ),
+    "pic_batched_stream_prepare": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,
+         ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p],
+    ),
+    "pic_batched_stream_segment": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "pic_batched_stream_status": (
+        ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]
+    ),
     "pic_graph_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "pic_graph_destroy": (ctypes.c_int, [ctypes.c_void_p]),
 }

@@ -48,6 +48,70 @@ MAX_ITEMS_PER_BLOCK = 1 << 16
 SOLO_MAX_GRIDS = 2
 
 
+# The streaming batched step (pic_batched_stream_*): 15 consumer warps of up to
+# three k-vectors each; a grid's tile is as many rows as those fill and a
+# ring stage of any grid stays under STREAM_STAGE_BYTES, so that four stages
+# fit in shared memory; about STREAM_ITEMS_PER_SM items per SM and global
+# step, which the CTAs take from a device-wide queue.
+STREAM_WARPS = 15
+STREAM_IPT = 3
+STREAM_STAGE_BYTES = 54 * 1024
+STREAM_ITEMS_PER_SM = 6
+
+
+def _stage_floats(tj: int, kp: int) -> int:
+    return 2 * (tj + 2) * kp + 2 * ((tj + 8) & ~3)
+
+
+def stream_tile_rows(no_xy: int, kpitch: int, warps: int = STREAM_WARPS) -> int:
+    """Interior rows of a grid's tiles in the streaming batched step."""
+    tj = max(1, min(int(no_xy) - 2, (STREAM_IPT * 32 * warps) // (int(kpitch) // 4)))
+    while tj > 1 and _stage_floats(tj, int(kpitch)) * 4 > STREAM_STAGE_BYTES:
+        tj -= 1
+    return tj
+
+
+def _stream_items(shapes, active, sms: int, warps: int = STREAM_WARPS):
+    """The work items of one streaming batched launch over the ``active``
+    grids (``shapes[c]`` = (no_xy, nzb, kpitch)): rows (grid, cj_lo, ci_lo,
+    ci_hi) that cover every interior row and plane of each active grid once,
+    grouped by grid, grids with the longest items first; and the tile rows of
+    every grid. Items are sized for about STREAM_ITEMS_PER_SM per SM."""
+    tile = np.array([stream_tile_rows(n, kp, warps) for n, _, kp in shapes], dtype=np.int32)
+    act = [int(c) for c in active]
+    vox = sum((shapes[c][0] - 2) ** 2 * (shapes[c][1] - 2) for c in act)
+    target = max(1.0, vox / (STREAM_ITEMS_PER_SM * max(1, sms)))
+    plan = []
+    for c in act:
+        n, nzb, _ = shapes[c]
+        tj = int(tile[c])
+        li = int(np.clip(np.ceil(target / (tj * (nzb - 2))), 2, n - 2))
+        ranges = -(-(n - 2) // li)
+        li = -(-(n - 2) // ranges)  # even split of the planes
+        plan.append((tj * li * nzb, c, tj, li))
+    rows = []
+    for _, c, tj, li in sorted(plan, key=lambda p: (-p[0], p[1])):
+        n = shapes[c][0]
+        for i0 in range(1, n - 1, li):
+            i1 = min(i0 + li, n - 1)
+            for j0 in range(1, n - 1, tj):
+                rows.append((c, j0, i0, i1))
+    return np.array(rows, dtype=np.int32).reshape(-1, 4), tile
+
+
+class PicBatchStream(ctypes.Structure):
+    _fields_ = [
+        ("n_cfgs", ctypes.c_int32),
+        ("n_items", ctypes.c_int32),
+        ("consumer_warps", ctypes.c_int32),
+        ("stages", ctypes.c_int32),
+        ("stage_floats", ctypes.c_int32),
+        ("ipt", ctypes.c_int32),
+        ("workspace", ctypes.c_void_p),
+        ("workspace_bytes", ctypes.c_int64),
+    ]
+
+
 def items_per_block(total_items: int, sms: int) -> int:
     """Work items per block for a phase of ``total_items`` items."""
     want = -(-int(total_items) // (WAVES * BLOCKS_PER_SM * max(1, sms)))
@@ -199,6 +263,7 @@ def run_batched_b200(
     progress: bool = False,
     persistent: bool = False,
     solo_grids: int = SOLO_MAX_GRIDS,
+    variant: str = "auto",
 ):
     """Simulate every configuration and return their Results, in order.
 
@@ -211,7 +276,11 @@ def run_batched_b200(
     64-configuration sweep the per-step launches are faster (1.31 vs 1.44 s):
     two device-wide barriers per step cost what two launch gaps do.
     Phases with at most ``solo_grids`` active grids run each grid's chunk
-    with the single-grid kernels instead (0: never).
+    with the single-grid kernels instead (0: never). ``variant`` picks the
+    fused step of the batched launches: "flat" (pic_batched_segment, neighbours
+    through L1/L2), "stream" (pic_batched_stream_segment: float32, planes staged
+    in a shared-memory ring, items from every grid taken from a device-wide
+    queue), or "auto" (stream for float32 batches without ``persistent``).
     """
     import torch
 
@@ -224,6 +293,10 @@ def run_batched_b200(
         raise ValueError("chunk_steps must be >= 1")
     if int(solo_grids) < 0:
         raise ValueError("solo_grids must be >= 0")
+    if variant not in ("auto", "flat", "stream"):
+        raise ValueError(f"variant must be 'auto', 'flat' or 'stream', got {variant!r}")
+    if variant == "stream" and (dtype != "float32" or persistent):
+        raise ValueError("the streaming batched step takes float32 batches without persistent launches")
     if not torch.cuda.is_available():
         raise RuntimeError("run_batched_b200 needs a CUDA device (a GB300); none is visible")
     lib = N.load()
@@ -317,6 +390,24 @@ def run_batched_b200(
     workspace = torch.zeros(int(wsb.value), dtype=torch.uint8, device=dev)
 
     st = torch.cuda.current_stream(dev).cuda_stream
+    use_stream = variant == "stream" or (variant == "auto" and dtype == "float32" and not persistent
+                                         and all(int(g.no_xy) >= 4 for g in grids))
+    stream_tabs = {}  # phase start -> (prepared PicBatchStream, its workspace)
+    if use_stream:
+        shapes = [(int(g.no_xy), int(g.nzb), int(g.kpitch)) for g in grids]
+        for s0, _, tab in phases:
+            if solo_grids > 0 and len(tab["active"]) <= solo_grids:
+                continue
+            items_h, tiles_h = _stream_items(shapes, tab["active"], sms)
+            sb = ctypes.c_int64()
+            N.check(lib.pic_batched_stream_workspace_bytes(n_cfg, len(items_h), STREAM_WARPS, ctypes.byref(sb)),
+                    "pic_batched_stream_workspace_bytes")
+            sws = torch.zeros(int(sb.value), dtype=torch.uint8, device=dev)
+            bs = PicBatchStream()
+            N.check(lib.pic_batched_stream_prepare(ctypes.addressof(cfg_arr), n_cfg, items_h.ctypes.data,
+                                                   len(items_h), tiles_h.ctypes.data, STREAM_WARPS, sws.data_ptr(),
+                                                   sws.numel(), st, ctypes.byref(bs)), "pic_batched_stream_prepare")
+            stream_tabs[s0] = (bs, sws)
     solo_ws = None
     if solo_grids > 0 and not persistent and any(len(t["active"]) <= solo_grids for _, _, t in phases):
         swb = ctypes.c_int64()
@@ -348,7 +439,8 @@ def run_batched_b200(
     stt_dev = torch.from_numpy(np.ascontiguousarray(step_tracks, dtype=np.int64)).to(dev)
     # chunks of global steps; chunk (c0, c1) needs grid c's tracks
     # [offsets[c][min(c0, T_c)], offsets[c][min(c1, T_c)])
-    chunks = [(c0, min(c0 + chunk_steps, s1), tab) for s0, s1, tab in phases for c0 in range(s0, s1, chunk_steps)]
+    chunks = [(c0, min(c0 + chunk_steps, s1), dict(tab, phase_start=s0)) for s0, s1, tab in phases
+              for c0 in range(s0, s1, chunk_steps)]
 
     def jobs_of(c0, c1):
         out = []
@@ -396,7 +488,11 @@ def run_batched_b200(
             L.counts, L.tally = counts.data_ptr(), tally.data_ptr()
             L.workspace, L.workspace_bytes = workspace.data_ptr(), workspace.numel()
             with nvtx_range(f"batched steps ({len(tab['active'])} grids)"):
-                if persistent:
+                if tab["phase_start"] in stream_tabs:
+                    bs = stream_tabs[tab["phase_start"]][0]
+                    N.check(lib.pic_batched_stream_segment(ctypes.byref(L), ctypes.byref(bs), st),
+                            "pic_batched_stream_segment")
+                elif persistent:
                     N.check(lib.pic_batched_persistent(ctypes.byref(L), sto_dev.data_ptr(), stt_dev.data_ptr(), st),
                             "pic_batched_persistent")
                 else:
@@ -413,6 +509,11 @@ def run_batched_b200(
             if sv.value != 0:
                 raise RuntimeError(f"a fused-step kernel gave up on a bounded wait (code {sv.value}); "
                                    "results are invalid")
+        for bs, _ in stream_tabs.values():
+            sv = ctypes.c_int32()
+            N.check(lib.pic_batched_stream_status(ctypes.byref(bs), 1, st, ctypes.byref(sv)), "pic_batched_stream_status")
+            if sv.value != 0:
+                raise RuntimeError(f"the streaming batched step gave up (status {sv.value}); results are invalid")
         if persistent and chunks:
             status = ctypes.c_int32()
             N.check(lib.pic_batched_status(ctypes.byref(L), st, ctypes.byref(status)), "pic_batched_status")

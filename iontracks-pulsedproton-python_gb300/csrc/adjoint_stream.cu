@@ -507,8 +507,10 @@ int launch_adjoint_stream(const pic_grid *g, const void *pos, const void *neg, c
     a.n_items = a.jt * ((a.n - 2 + a.li - 1) / a.li);
     a.stages = kAdjStreamStages;
     a.consumer_warps = kAdjStreamWarps;
-    a.p_lat = (float)g->p_lat; a.p_zm = (float)g->p_zm; a.p_zp = (float)g->p_zp; a.p_cen = (float)g->p_cen;
-    a.n_lat = (float)g->n_lat; a.n_zm = (float)g->n_zm; a.n_zp = (float)g->n_zp; a.n_cen = (float)g->n_cen;
+    a.p_lat = (float)g->p_lat; a.p_zm = (float)g->p_zm; a.p_zp = (float)g->p_zp;
+    a.p_cen = centre_weight<float>(g->p_lat, g->p_zm, g->p_zp, g->p_cen);
+    a.n_lat = (float)g->n_lat; a.n_zm = (float)g->n_zm; a.n_zp = (float)g->n_zp;
+    a.n_cen = centre_weight<float>(g->n_lat, g->n_zm, g->n_zp, g->n_cen);
     a.a = (float)g->alpha_dt;
     a.c_pos = (float)(g->p_zm - g->p_zp);
     a.c_neg = (float)(g->n_zm - g->n_zp);

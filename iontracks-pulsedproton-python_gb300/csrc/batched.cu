@@ -71,8 +71,10 @@ __device__ void grid_args(const pic_batch_cfg &C, StepArgs<T> &a) {
     a.nze = (int)g.nze;
     a.gap_end = (int)(g.nze + g.no_z);
     a.reflecting = g.wall == PIC_WALL_REFLECTING;
-    a.p_lat = (T)g.p_lat; a.p_zm = (T)g.p_zm; a.p_zp = (T)g.p_zp; a.p_cen = (T)g.p_cen;
-    a.n_lat = (T)g.n_lat; a.n_zm = (T)g.n_zm; a.n_zp = (T)g.n_zp; a.n_cen = (T)g.n_cen;
+    a.p_lat = (T)g.p_lat; a.p_zm = (T)g.p_zm; a.p_zp = (T)g.p_zp;
+    a.p_cen = centre_weight<T>(g.p_lat, g.p_zm, g.p_zp, g.p_cen);
+    a.n_lat = (T)g.n_lat; a.n_zm = (T)g.n_zm; a.n_zp = (T)g.n_zp;
+    a.n_cen = centre_weight<T>(g.n_lat, g.n_zm, g.n_zp, g.n_cen);
     a.alpha_dt = (T)g.alpha_dt;
     a.gfac = (T)g.gaussian_factor;
     a.score.two_mid = (int64_t)(2.0 * g.mid_xy);
@@ -394,12 +396,14 @@ static void launch_batched_step(const BatchLaunch &L, int bi, int bo, double *pa
     batched_step_kernel<T, BLOCK, I><<<(unsigned)L.n_blocks, BLOCK, 0, st>>>(b);
 }
 
-int batched_loop(const BatchLaunch &L, cudaStream_t st) {
+int batched_loop(const BatchLaunch &L, cudaStream_t st) { return batched_loop_stream(L, nullptr, st); }
+
+int batched_loop_stream(const BatchLaunch &L, const pic_batch_stream *B, cudaStream_t st) {
     constexpr int WARPS = 8;
-    unsigned int *counters = reinterpret_cast<unsigned int *>(L.workspace);
-    double *partials = partials_of(L);
+    unsigned int *counters = B ? nullptr : reinterpret_cast<unsigned int *>(L.workspace);
+    double *partials = B ? nullptr : partials_of(L);
     const int sms = sm_count();
-    if (L.n_steps > 0) {
+    if (L.n_steps > 0 && !B) {
         int rc = L.dtype == PIC_F64 ? prep_table<double>(L, st) : prep_table<float>(L, st);
         if (rc) return rc;
     }
@@ -421,6 +425,11 @@ int batched_loop(const BatchLaunch &L, cudaStream_t st) {
                     L.ys, (float2 *)L.dens[bi], L.counts, parts);
             int rc = check_launch("batched_deposit_kernel");
             if (rc) return rc;
+        }
+        if (B) {
+            int rc = batched_stream_step(L, *B, bi, bo, step, st);
+            if (rc) return rc;
+            continue;
         }
         if (L.dtype == PIC_F64) {
             if (L.index32) launch_batched_step<double, uint32_t>(L, bi, bo, partials, counters, step, st);

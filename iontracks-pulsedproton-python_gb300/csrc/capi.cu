@@ -231,20 +231,16 @@ static int check_segment(const pic_grid *g, void *pos0, void *neg0, void *pos1, 
     return PIC_OK;
 }
 
-static int check_batch(const pic_batch_launch *L) {
+// What every batched launch needs: buffers, step range and task tables.
+static int check_batch_common(const pic_batch_launch *L) {
     if (!L) return set_error(PIC_E_INVALID, "launch descriptor is null");
     if (L->dtype != PIC_F32 && L->dtype != PIC_F64) return set_error(PIC_E_INVALID, "dtype must be PIC_F32 or PIC_F64");
-    if (L->n_cfgs < 1 || L->n_blocks < 1) return set_error(PIC_E_INVALID, "n_cfgs and n_blocks must be >= 1");
+    if (L->n_cfgs < 1) return set_error(PIC_E_INVALID, "n_cfgs must be >= 1");
     if (L->n_steps < 0 || L->first_step < 0) return set_error(PIC_E_INVALID, "step range must be non-negative");
-    if (L->index32 != 0 && L->index32 != 1) return set_error(PIC_E_INVALID, "index32 must be 0 or 1");
-    if (!L->cfgs || !L->blk_cfg || !L->blk_item0 || !L->blk_item1 || !L->cfg_blk0 || !L->cfg_nblk || !L->counts ||
-        !L->tally || !L->workspace || !L->dens[0] || !L->dens[1])
+    if (!L->cfgs || !L->counts || !L->tally || !L->dens[0] || !L->dens[1])
         return set_error(PIC_E_INVALID, "null pointer in the batch launch descriptor");
     int rc = check_fields(L->pos[0], L->neg[0], L->pos[1], L->neg[1]);
     if (rc) return rc;
-    int64_t need = 0;
-    if ((rc = batched_workspace_bytes(L->n_blocks, L->n_cfgs, &need))) return rc;
-    if (L->workspace_bytes < need) return set_error(PIC_E_INVALID, "workspace too small (pic_batched_workspace_bytes)");
     if (!L->step_task_off || !L->step_tracks) return set_error(PIC_E_INVALID, "step task tables are null");
     for (int64_t s = 0; s < L->n_steps; ++s) {
         if (L->step_task_off[s + 1] < L->step_task_off[s] || L->step_tracks[s] < 0)
@@ -252,6 +248,19 @@ static int check_batch(const pic_batch_launch *L) {
         if (L->step_tracks[s] > 0 && (!L->task_cfg || !L->task_first || !L->task_prefix || !L->xs || !L->ys))
             return set_error(PIC_E_INVALID, "track or task arrays are null");
     }
+    return PIC_OK;
+}
+
+static int check_batch(const pic_batch_launch *L) {
+    int rc = check_batch_common(L);
+    if (rc) return rc;
+    if (L->n_blocks < 1) return set_error(PIC_E_INVALID, "n_cfgs and n_blocks must be >= 1");
+    if (L->index32 != 0 && L->index32 != 1) return set_error(PIC_E_INVALID, "index32 must be 0 or 1");
+    if (!L->blk_cfg || !L->blk_item0 || !L->blk_item1 || !L->cfg_blk0 || !L->cfg_nblk || !L->workspace)
+        return set_error(PIC_E_INVALID, "null pointer in the batch launch descriptor");
+    int64_t need = 0;
+    if ((rc = batched_workspace_bytes(L->n_blocks, L->n_cfgs, &need))) return rc;
+    if (L->workspace_bytes < need) return set_error(PIC_E_INVALID, "workspace too small (pic_batched_workspace_bytes)");
     return PIC_OK;
 }
 
@@ -734,6 +743,37 @@ int pic_batched_persistent(const pic_batch_launch *launch, const int64_t *step_t
 int pic_batched_status(const pic_batch_launch *launch, uintptr_t stream, int32_t *status) {
     if (!launch || !launch->workspace || !status) return set_error(PIC_E_INVALID, "null pointer argument");
     return batched_status(*launch, reinterpret_cast<cudaStream_t>(stream), status);
+}
+
+int pic_batched_stream_workspace_bytes(int32_t n_cfgs, int32_t n_items, int32_t consumer_warps, int64_t *bytes) {
+    if (!bytes) return set_error(PIC_E_INVALID, "bytes is null");
+    return batched_stream_workspace_bytes(n_cfgs, n_items, consumer_warps, bytes);
+}
+
+int pic_batched_stream_prepare(const pic_batch_cfg *cfgs_host, int32_t n_cfgs, const int32_t *items_host,
+                               int32_t n_items, const int32_t *tile_rows_host, int32_t consumer_warps,
+                               void *workspace, int64_t workspace_bytes, uintptr_t stream, pic_batch_stream *out) {
+    NvtxRange nvtx_range("pic_batched_stream_prepare");
+    return batched_stream_prepare(cfgs_host, n_cfgs, items_host, n_items, tile_rows_host, consumer_warps, workspace,
+                                  workspace_bytes, reinterpret_cast<cudaStream_t>(stream), out);
+}
+
+int pic_batched_stream_segment(const pic_batch_launch *launch, const pic_batch_stream *bs, uintptr_t stream) {
+    NvtxRange nvtx_range("pic_batched_stream_segment");
+    int rc = check_batch_common(launch);
+    if (rc) return rc;
+    if (!bs || !bs->workspace) return set_error(PIC_E_INVALID, "prepared stream tables are null");
+    if (launch->dtype != PIC_F32) return set_error(PIC_E_INVALID, "the batched streaming step takes float32 batches");
+    if (bs->n_cfgs != launch->n_cfgs) return set_error(PIC_E_INVALID, "prepared tables are for another batch");
+    if (bs->n_items < 1 || bs->consumer_warps < 1 || bs->consumer_warps > 15 || bs->stages < 4 ||
+        bs->ipt < 1 || bs->ipt > 3 || bs->stage_floats < 1)
+        return set_error(PIC_E_INVALID, "pic_batch_stream was not filled by pic_batched_stream_prepare");
+    return batched_loop_stream(*launch, bs, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int pic_batched_stream_status(const pic_batch_stream *bs, int32_t reset, uintptr_t stream, int32_t *status) {
+    if (!bs || !bs->workspace || !status) return set_error(PIC_E_INVALID, "null pointer argument");
+    return batched_stream_status(*bs, reset, reinterpret_cast<cudaStream_t>(stream), status);
 }
 
 int pic_batched_graph_create(const pic_batch_launch *launch, uintptr_t stream, uintptr_t *graph_out) {

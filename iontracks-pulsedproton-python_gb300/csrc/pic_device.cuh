@@ -11,6 +11,21 @@
 
 namespace pic {
 
+// The centre weight of the Lax-Wendroff stencil in the field type. The four
+// weights sum to one (zm + zp + 4 lat + cen = 1: the scheme conserves carriers
+// between recombination and collection). Rounded one by one to float32 they
+// sum to 1 + O(3e-8), and that bias acts on every voxel at every step: over
+// the few hundred steps a carrier lives it shifts the densities, and through
+// the recombination term k_s, by ~1e-5. So the float32 centre weight absorbs
+// the rounding of the other three, leaving the float32 sum within half an ulp
+// of cen (~1e-9) of the float64 one; float64 fields take cen as it is.
+template <typename T>
+__host__ __device__ inline T centre_weight(double lat, double zm, double zp, double cen) {
+    if (sizeof(T) == sizeof(double)) return (T)cen;
+    const double d = ((double)(float)zm - zm) + ((double)(float)zp - zp) + 4.0 * ((double)(float)lat - lat);
+    return (T)(cen - d);
+}
+
 // Four consecutive k elements of one (i, j) column. The field rows are
 // 32-byte aligned (kpitch is a multiple of 8) and every vector starts at a
 // multiple of 4 elements, so float loads are single 128-bit accesses and

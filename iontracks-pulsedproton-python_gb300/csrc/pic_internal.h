@@ -146,6 +146,16 @@ int batched_loop(const BatchLaunch &L, cudaStream_t st);
 int batched_persistent(const BatchLaunch &L, const int64_t *step_task_off, const int64_t *step_tracks,
                        cudaStream_t st);
 int batched_status(const BatchLaunch &L, cudaStream_t st, int32_t *status);
+// The streaming batched step (batched_stream.cu).
+int batched_stream_workspace_bytes(int32_t n_cfgs, int32_t n_items, int32_t consumer_warps, int64_t *bytes);
+int batched_stream_prepare(const pic_batch_cfg *cfgs, int32_t n_cfgs, const int32_t *items, int32_t n_items,
+                           const int32_t *tile_rows, int32_t consumer_warps, void *ws, int64_t ws_bytes,
+                           cudaStream_t st, pic_batch_stream *out);
+int batched_stream_step(const BatchLaunch &L, const pic_batch_stream &B, int bi, int bo, int64_t step,
+                        cudaStream_t st);
+int batched_stream_status(const pic_batch_stream &B, int32_t reset, cudaStream_t st, int32_t *status);
+// batched_loop with B non-null runs the streaming step instead of the flat one.
+int batched_loop_stream(const BatchLaunch &L, const pic_batch_stream *B, cudaStream_t st);
 
 // Several steps of one grid per cooperative launch (multistep.cu): for a
 // resolved FLAT grid with steps_per_launch > 1.

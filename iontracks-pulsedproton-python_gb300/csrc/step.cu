@@ -71,8 +71,10 @@ static int launch_step_t(const pic_grid *g, const void *pos_in, const void *neg_
     a.nze = (int)g->nze;
     a.gap_end = (int)(g->nze + g->no_z);
     a.reflecting = g->wall == PIC_WALL_REFLECTING;
-    a.p_lat = (T)g->p_lat; a.p_zm = (T)g->p_zm; a.p_zp = (T)g->p_zp; a.p_cen = (T)g->p_cen;
-    a.n_lat = (T)g->n_lat; a.n_zm = (T)g->n_zm; a.n_zp = (T)g->n_zp; a.n_cen = (T)g->n_cen;
+    a.p_lat = (T)g->p_lat; a.p_zm = (T)g->p_zm; a.p_zp = (T)g->p_zp;
+    a.p_cen = centre_weight<T>(g->p_lat, g->p_zm, g->p_zp, g->p_cen);
+    a.n_lat = (T)g->n_lat; a.n_zm = (T)g->n_zm; a.n_zp = (T)g->n_zp;
+    a.n_cen = centre_weight<T>(g->n_lat, g->n_zm, g->n_zp, g->n_cen);
     a.alpha_dt = (T)g->alpha_dt;
     a.gfac = (T)g->gaussian_factor;
     int rc = score_test(g, &a.score);
