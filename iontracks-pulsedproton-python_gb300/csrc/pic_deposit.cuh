@@ -16,8 +16,6 @@ __device__ __forceinline__ float gauss1(double d, float h2b2) {
     return expf(-(f * f) * h2b2);
 }
 __device__ __forceinline__ double gauss1(double d, double h2b2) { return exp(-(d * d) * h2b2); }
-__device__ __forceinline__ float exp_neg(float a) { return expf(-a); }
-__device__ __forceinline__ double exp_neg(double a) { return exp(-a); }
 
 __device__ __forceinline__ void add_pair(float2 *p, float c, float l) { atomicAdd(p, make_float2(c, l)); }
 __device__ __forceinline__ void add_pair(double2 *p, double c, double l) {
@@ -93,141 +91,6 @@ __device__ __forceinline__ void deposit_track(double x, double y, int64_t n, int
                 if (jok && (c != T(0) || l != T(0))) add_pair(dens + (i0 + (int64_t)nparts * r) * dp + j, c, l);
             }
         }
-    }
-}
-
-// ---------------------------------------------------------------------------
-// Tile form of the deposition, for grids whose tracks overlap heavily (a small
-// grid with hundreds of tracks a step: the per-track form's atomics all land
-// on the same few hundred cells and serialise in L2). A block owns a
-// kDepTile x kDepTile tile of the pairs and a range of the step's tracks:
-// it keeps the tracks whose written box meets the tile (in track order), and
-// each thread sums them over its four cells in registers, then adds each
-// cell's sum once. The per-track terms are those of deposit_track (the same
-// factors, G g_j on the column side); only the order of the additions
-// differs. With one part per tile the sums are deterministic.
-constexpr int kDepTile = 32;     // cells per tile side
-constexpr int kDepThreads = 256; // a thread owns 4 adjacent cells of one tile row
-constexpr int kDepBatch = 8;     // tracks whose factors are staged together
-
-__host__ __device__ inline int64_t deposit_tiles(int64_t n) {
-    const int64_t t = (n + kDepTile - 1) / kDepTile;
-    return t * t;
-}
-// Parts a tile's tracks are split into (each part is one block): one per 256
-// tracks, at most 8, so a heavily hit tile is summed by several SMs.
-__host__ __device__ inline int deposit_tile_parts(int64_t m) {
-    const int64_t p = (m + 255) / 256;
-    return (int)(p < 1 ? 1 : (p > 8 ? 8 : p));
-}
-
-template <typename T>
-struct DepTileShared {
-    int sel[kDepThreads];        // tracks of the current chunk that meet the tile (offsets from t0)
-    int wcount[kDepThreads / 32];
-    int lo[kDepBatch][2], hi[kDepBatch][2], ci[kDepBatch][2];  // truncation box and centre cell per axis
-    T cf[kDepBatch][2];          // centre minus its cell, in [0, 1)
-    T fac[kDepBatch][2][kDepTile + 2];  // g_i over rows i0-1 .. i0+kDepTile; G g_j over the columns
-};
-
-// Tracks [t0, t1) of the step into tile `tile` (row-major over the
-// ceil(n / kDepTile)^2 tiles) of the pairs; counts (if non-null) once per
-// track by the tile holding its centre column.
-template <typename T>
-__device__ __forceinline__ void deposit_tile(const double *__restrict__ xs, const double *__restrict__ ys, int64_t t0,
-                                             int64_t t1, int64_t n, int64_t dp, double cut, T h2b2, T gfac,
-                                             pair_t<T> *__restrict__ dens, uint32_t *__restrict__ counts, int64_t tile,
-                                             DepTileShared<T> &sh) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int64_t tr = (n + kDepTile - 1) / kDepTile;
-    const int64_t i0 = (tile / tr) * kDepTile, j0 = (tile % tr) * kDepTile;
-    const int r = threadIdx.x >> 3, cg = (threadIdx.x & 7) * 4;  // this thread's row and first column in the tile
-    T acc_c[4] = {T(0), T(0), T(0), T(0)}, acc_l[4] = {T(0), T(0), T(0), T(0)};
-    // conservative reach of a track's written box (truncation box widened by
-    // one cell, plus a margin for the float test)
-    const float reach = (float)cut + 2.0f;
-    for (int64_t c0 = t0; c0 < t1; c0 += kDepThreads) {
-        const int64_t t = c0 + threadIdx.x;
-        bool hit = false;
-        if (t < t1) {
-            const double x = xs[t], y = ys[t];
-            if (counts) {
-                const int64_t ix = (int64_t)x, iy = (int64_t)y;  // int() floors for centres in [0, n)
-                if (ix >= i0 && ix < i0 + kDepTile && iy >= j0 && iy < j0 + kDepTile && ix < n && iy < n)
-                    atomicAdd(counts + ix * n + iy, 1u);
-            }
-            const float xf = (float)x, yf = (float)y;
-            hit = xf + reach >= (float)i0 && xf - reach <= (float)(i0 + kDepTile - 1) && yf + reach >= (float)j0 &&
-                  yf - reach <= (float)(j0 + kDepTile - 1);
-        }
-        // order-preserving compaction of this chunk's hits
-        const unsigned bal = __ballot_sync(0xffffffffu, hit);
-        if (lane == 0) sh.wcount[warp] = __popc(bal);
-        __syncthreads();
-        int base = 0, total = 0;
-#pragma unroll
-        for (int w = 0; w < kDepThreads / 32; ++w) {
-            base += w < warp ? sh.wcount[w] : 0;
-            total += sh.wcount[w];
-        }
-        if (hit) sh.sel[base + __popc(bal & ((1u << lane) - 1u))] = (int)(t - t0);
-        __syncthreads();
-        for (int b = 0; b < total; b += kDepBatch) {
-            const int kb = total - b < kDepBatch ? total - b : kDepBatch;
-            // per track and axis: the truncation box [ceil(c - cut), floor(c + cut)]
-            // clipped to the grid (solver_numba.py:86-89), the centre's cell and
-            // its offset in it (float64 once per track, the field type after)
-            if (threadIdx.x < 2 * kDepBatch) {
-                const int k = threadIdx.x >> 1, ax = threadIdx.x & 1;
-                if (k < kb) {
-                    const double c = ax ? ys[t0 + sh.sel[b + k]] : xs[t0 + sh.sel[b + k]];
-                    const int64_t lo = (int64_t)ceil(c - cut), hi = (int64_t)floor(c + cut) + 1;
-                    const double fl = floor(c);
-                    sh.lo[k][ax] = (int)(lo < 0 ? 0 : lo);
-                    sh.hi[k][ax] = (int)(hi > n ? n : hi);
-                    sh.ci[k][ax] = (int)fl;
-                    sh.cf[k][ax] = (T)(c - fl);
-                }
-            }
-            __syncthreads();
-            // the factors of the batch: g at offsets (cell - ci) - cf, an exact
-            // integer less the centre's fraction, rounded once to the field
-            // type as deposit_track rounds its float64 offset
-            for (int q = threadIdx.x; q < kDepBatch * 2 * (kDepTile + 2); q += kDepThreads) {
-                const int k = q / (2 * (kDepTile + 2)), rem = q - k * 2 * (kDepTile + 2);
-                const int ax = rem / (kDepTile + 2), e = rem - ax * (kDepTile + 2);
-                T v = T(0);
-                if (k < kb) {
-                    const int cell = (int)(ax ? j0 : i0) - 1 + e;
-                    if (cell >= sh.lo[k][ax] && cell < sh.hi[k][ax]) {
-                        const T d = (T)(cell - sh.ci[k][ax]) - sh.cf[k][ax];
-                        v = exp_neg(d * d * h2b2);
-                        if (ax) v *= gfac;
-                    }
-                }
-                sh.fac[k][ax][e] = v;
-            }
-            __syncthreads();
-            for (int k = 0; k < kb; ++k) {
-                const T gm = sh.fac[k][0][r], g0 = sh.fac[k][0][r + 1], gp = sh.fac[k][0][r + 2];
-                const T hsum = gm + gp;
-#pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const T Gj = sh.fac[k][1][cg + e + 1];
-                    const T Hj = sh.fac[k][1][cg + e] + sh.fac[k][1][cg + e + 2];
-                    acc_c[e] += g0 * Gj;
-                    acc_l[e] += hsum * Gj + g0 * Hj;
-                }
-            }
-            __syncthreads();
-        }
-    }
-    const int64_t i = i0 + r;
-    if (i >= n) return;
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-        const int64_t j = j0 + cg + e;
-        if (j < n && (acc_c[e] != T(0) || acc_l[e] != T(0))) add_pair(dens + i * dp + j, acc_c[e], acc_l[e]);
     }
 }
 
