@@ -410,8 +410,9 @@ int pic_graph_destroy(uintptr_t graph);
  * pic_batch_cfg entry (its pic_grid scalars -- launch-shape fields ignored --
  * and its offsets). One global step advances every active grid by one of its
  * own time steps, with two launches for the whole batch: a deposition over
- * the step's tracks of all grids (a task list maps warps to grids and
- * tracks) and the flat fused step over a work table that gives each block
+ * the step's tracks of all grids (a task list gives each grid's tracks; each
+ * 64 x 64 tile of a grid's deposition sums the tracks that reach it) and the
+ * flat fused step over a work table that gives each block
  * one grid and a contiguous range of that grid's items (a grid's blocks are
  * consecutive; its last block to finish writes its tallies). Grids that have
  * finished are left out of the work table and task list of later steps.
@@ -442,10 +443,14 @@ typedef struct pic_batch_launch {
     void *dens[2];                         /* device, packed deposition pairs, by step parity */
     const double *xs, *ys;                 /* device, packed track centres                   */
     const int32_t *task_cfg;               /* device, per task (grid, tracks of one step):   */
-    const int64_t *task_first;             /*   grid, first track, and first warp within the */
-    const int64_t *task_prefix;            /*   step's deposition launch                     */
+    const int64_t *task_first;             /*   grid, first track, and the step's tracks     */
+    const int64_t *task_prefix;            /*   before the task                              */
     const int64_t *step_task_off;          /* host, n_steps + 1: the steps' task ranges      */
     const int64_t *step_tracks;            /* host, n_steps: tracks deposited in each step   */
+    const int64_t *step_blocks;            /* host, n_steps: blocks of each step's           */
+                                           /*  deposition, the sum over its tasks of         */
+                                           /*  ceil(no_xy/64)^2 x min(32, max(1, ceil(tracks */
+                                           /*  of the task / 32)))                           */
     int64_t first_step, n_steps;           /* global steps [first_step, first_step+n_steps)  */
     uint32_t *counts;                      /* device, packed track histograms                */
     double *tally;                         /* device, packed [rows][4] tallies               */

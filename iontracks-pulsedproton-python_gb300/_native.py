@@ -24,7 +24,7 @@ PIC_VARIANT_AUTO = 0
 PIC_VARIANT_FLAT = 1
 PIC_VARIANT_STREAM = 2
 # pic_abi_version() of the library these structures mirror
-ABI_VERSION = 4
+ABI_VERSION = 5
 
 _LIB_PATH = Path(__file__).resolve().parent / "_build" / "libpic_gb300.so"
 _lock = threading.Lock()

@@ -151,6 +151,7 @@ class PicBatchLaunch(ctypes.Structure):
         ("task_prefix", ctypes.c_void_p),
         ("step_task_off", ctypes.c_void_p),
         ("step_tracks", ctypes.c_void_p),
+        ("step_blocks", ctypes.c_void_p),
         ("first_step", ctypes.c_int64),
         ("n_steps", ctypes.c_int64),
         ("counts", ctypes.c_void_p),
@@ -204,17 +205,30 @@ def _phases(total_steps: Sequence[int]):
     return phases
 
 
-def _task_tables(offsets, totals, track_base):
+DEP_TILE = 64  # cells per side of a deposition tile (pic_deposit.cuh, kDepTile)
+
+
+def deposit_blocks(no_xy, tracks):
+    """Blocks of the tile-form deposition of one grid's tracks in one step:
+    tiles x parts, parts = one per 32 tracks, 1 to 32 (pic_deposit.cuh,
+    deposit_tiles / deposit_tile_parts)."""
+    tiles = (-(-np.asarray(no_xy, dtype=np.int64) // DEP_TILE)) ** 2
+    parts = np.clip(-(-np.asarray(tracks, dtype=np.int64) // 32), 1, 32)
+    return tiles * parts
+
+
+def _task_tables(offsets, totals, track_base, no_xy=None):
     """The deposition tasks of every global step, in grid order within a step.
 
     ``offsets[c]`` = grid c's cumulative track counts per step (length
     ``totals[c] + 1``), ``track_base[c]`` = its first track in the packed
     track arrays. Returns ``(step_task_off, step_tracks, task_cfg,
-    task_first, task_prefix)``: the tasks of step s are ``step_task_off[s] ..
-    step_task_off[s + 1] - 1``, one per grid with tracks at s, giving the
-    grid, its first packed track and the tracks of the step's earlier tasks
-    (one warp group per track, so the warps before it); ``step_tracks[s]`` =
-    all tracks of step s."""
+    task_first, task_prefix, step_blocks)``: the tasks of step s are
+    ``step_task_off[s] .. step_task_off[s + 1] - 1``, one per grid with tracks
+    at s, giving the grid, its first packed track and the tracks of the step's
+    earlier tasks; ``step_tracks[s]`` = all tracks of step s,
+    ``step_blocks[s]`` = the blocks of its tile-form deposition (grid sizes
+    ``no_xy[c]``; zeros when not given)."""
     n_cfg = len(offsets)
     S = max(totals)
     M = np.zeros((S, n_cfg), dtype=np.int64)  # tracks of grid c at global step s
@@ -229,7 +243,10 @@ def _task_tables(offsets, totals, track_base):
     step_tracks = M.sum(axis=1)
     excl = np.cumsum(vals) - vals  # tracks before each task, over all steps
     t_prefix = excl - excl[step_task_off[s_idx]] if len(vals) else excl
-    return step_task_off, step_tracks, c_idx.astype(np.int32), F[s_idx, c_idx], t_prefix
+    step_blocks = np.zeros(S, dtype=np.int64)
+    if no_xy is not None and len(vals):
+        np.add.at(step_blocks, s_idx, deposit_blocks(np.asarray(no_xy)[c_idx], vals))
+    return step_task_off, step_tracks, c_idx.astype(np.int32), F[s_idx, c_idx], t_prefix, step_blocks
 
 
 def _work_table(items, active, sms: int) -> dict:
@@ -368,7 +385,8 @@ def run_batched_b200(
     # --- per global step: tasks (grid, first track, first warp), in grid
     # order within a step
     S = max(totals)
-    step_task_off, step_tracks, t_cfg, t_first, t_prefix = _task_tables(offsets, totals, track_base)
+    step_task_off, step_tracks, t_cfg, t_first, t_prefix, step_blocks = _task_tables(
+        offsets, totals, track_base, [int(g.no_xy) for g in grids])
     one = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a if len(a) else np.zeros(1), dtype=dt)).to(dev)
     task_cfg = one(t_cfg, np.int32)
     task_first = one(t_first, np.int64)
@@ -483,8 +501,10 @@ def run_batched_b200(
             L.task_cfg, L.task_first, L.task_prefix = task_cfg.data_ptr(), task_first.data_ptr(), task_prefix.data_ptr()
             sto = np.ascontiguousarray(step_task_off[c0 : c1 + 1])
             stt = np.ascontiguousarray(step_tracks[c0:c1])
+            stb = np.ascontiguousarray(step_blocks[c0:c1])
             L.step_task_off = sto.ctypes.data
             L.step_tracks = stt.ctypes.data
+            L.step_blocks = stb.ctypes.data
             L.first_step, L.n_steps = c0, c1 - c0
             L.counts, L.tally = counts.data_ptr(), tally.data_ptr()
             L.workspace, L.workspace_bytes = workspace.data_ptr(), workspace.numel()

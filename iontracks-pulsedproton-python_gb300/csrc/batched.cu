@@ -5,8 +5,9 @@
 // pic_batch_cfg entries (each grid's pic_grid scalars and offsets). One global
 // step advances every active grid by one of its own time steps with two
 // launches for the whole batch:
-//   * batched_deposit_kernel -- one warp per track of this step, over the
-//     tracks of every grid (a task list maps warp -> grid, track);
+//   * batched_deposit_kernel -- the tile form of the deposition (pic_deposit.cuh)
+//     over the tracks of every grid: a task list gives each grid's tracks of
+//     the step, each task takes its grid's tiles times its parts of blocks;
 //   * batched_step_kernel -- the flat fused step (pic_flat.cuh) over a work
 //     table that gives each block one grid and a contiguous range of that
 //     grid's items; a grid's blocks are consecutive in the table, and the
@@ -192,38 +193,59 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 4 : 1) batched_step_ke
     batched_step_block<T, BLOCK, I>(b, blockIdx.x, red, last, a);
 }
 
-// Warp w of a global step's deposition: the track it owns, found in the
-// step's task list (grid, first track, first warp) by binary search.
+// Block `blk` of a global step's deposition (the tile form of
+// pic_deposit.cuh): the step's tasks (grid, first track, tracks before it) are
+// scanned in order, each taking tiles(grid) x parts(its tracks) blocks, to
+// find this block's task, tile and part. `total` = the step's tracks.
 template <typename T>
-__device__ __forceinline__ void batched_deposit_warp(const pic_batch_cfg *cfgs, const int32_t *task_cfg,
-                                                     const int64_t *task_first, const int64_t *task_prefix,
-                                                     int n_tasks, int64_t w, const double *xs, const double *ys,
-                                                     pair_t<T> *dens, uint32_t *counts, int lane, int part,
-                                                     int nparts) {
-    int lo = 0, hi = n_tasks - 1;  // last task whose first warp is <= w
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (task_prefix[mid] <= w) lo = mid; else hi = mid - 1;
+__device__ __forceinline__ void batched_deposit_block(const pic_batch_cfg *cfgs, const int32_t *task_cfg,
+                                                      const int64_t *task_first, const int64_t *task_prefix,
+                                                      int n_tasks, int64_t total, int64_t blk, const double *xs,
+                                                      const double *ys, pair_t<T> *dens, uint32_t *counts,
+                                                      DepTileShared<T> &sh) {
+    int64_t acc = 0;
+    for (int t = 0; t < n_tasks; ++t) {
+        const int64_t m = (t + 1 < n_tasks ? task_prefix[t + 1] : total) - task_prefix[t];
+        const pic_batch_cfg &C = cfgs[task_cfg[t]];
+        const int64_t n = C.grid.no_xy;
+        const int parts = deposit_tile_parts(m);
+        const int64_t nb = deposit_tiles(n) * parts;
+        if (blk < acc + nb) {
+            const int64_t local = blk - acc, tile = local / parts;
+            const int part = (int)(local % parts);
+            const int64_t f = task_first[t];
+            deposit_tile<T>(xs + f, ys + f, m * part / parts, m * (part + 1) / parts, n, (n + 3) / 4 * 4,
+                            C.grid.cutoff_voxels, (T)C.grid.h2_over_b2, (T)C.grid.gaussian_factor,
+                            dens + C.dens_off, counts + C.counts_off, tile, sh);
+            return;
+        }
+        acc += nb;
     }
-    const pic_batch_cfg &C = cfgs[task_cfg[lo]];
-    const int64_t idx = task_first[lo] + (w - task_prefix[lo]);
-    const int64_t n = C.grid.no_xy;
-    deposit_track<T>(xs[idx], ys[idx], n, (n + 3) / 4 * 4, C.grid.cutoff_voxels, (T)C.grid.h2_over_b2,
-                     (T)C.grid.gaussian_factor, dens + C.dens_off, counts + C.counts_off, lane, part, nparts);
 }
 
-template <typename T, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) batched_deposit_kernel(const pic_batch_cfg *cfgs,
-                                                                      const int32_t *task_cfg,
-                                                                      const int64_t *task_first,
-                                                                      const int64_t *task_prefix, int n_tasks,
-                                                                      int64_t total, const double *xs,
-                                                                      const double *ys, pair_t<T> *dens,
-                                                                      uint32_t *counts, int parts) {
-    const int64_t w = (int64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);  // `parts` warps per track
-    if (w >= total * parts) return;
-    batched_deposit_warp<T>(cfgs, task_cfg, task_first, task_prefix, n_tasks, w / parts, xs, ys, dens, counts,
-                            threadIdx.x & 31, (int)(w % parts), parts);
+template <typename T>
+__global__ void __launch_bounds__(kDepThreads) batched_deposit_kernel(const pic_batch_cfg *cfgs,
+                                                                       const int32_t *task_cfg,
+                                                                       const int64_t *task_first,
+                                                                       const int64_t *task_prefix, int n_tasks,
+                                                                       int64_t total, const double *xs,
+                                                                       const double *ys, pair_t<T> *dens,
+                                                                       uint32_t *counts) {
+    __shared__ DepTileShared<T> sh;
+    batched_deposit_block<T>(cfgs, task_cfg, task_first, task_prefix, n_tasks, total, blockIdx.x, xs, ys, dens,
+                             counts, sh);
+}
+
+// Blocks of one global step's deposition (every thread of the persistent
+// kernel forms the same number; the per-step launches take the host's).
+__device__ __forceinline__ int64_t batched_deposit_blocks(const pic_batch_cfg *cfgs, const int32_t *task_cfg,
+                                                          const int64_t *task_prefix, int n_tasks, int64_t total) {
+    int64_t acc = 0;
+    for (int t = 0; t < n_tasks; ++t) {
+        const int64_t m = (t + 1 < n_tasks ? task_prefix[t + 1] : total) - task_prefix[t];
+        acc += deposit_tiles(cfgs[task_cfg[t]].grid.no_xy) * deposit_tile_parts(m);
+    }
+    return acc;
 }
 
 // Workspace layout: [per-grid completion counters, n_cfgs x u32, padded to
@@ -296,16 +318,19 @@ __global__ void __launch_bounds__(256) batched_persistent_kernel(BatchPersistArg
     __shared__ typename RedT<T>::type red[BLOCK / 32][4];
     __shared__ bool last;
     __shared__ StepArgs<T> a;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __shared__ DepTileShared<T> dep;
+    static_assert(BLOCK == kDepThreads, "the persistent kernel's blocks run the tile deposition");
     for (int64_t s = p.first_step; s < p.first_step + p.n_steps; ++s) {
         const int bi = (int)(s & 1), bo = bi ^ 1;
         const int64_t t0 = p.step_task_off[s], t1 = p.step_task_off[s + 1], tracks = p.step_tracks[s];
         if (tracks > 0 && t1 > t0) {
-            const int parts = deposit_parts(tracks, p.sms);
-            for (int64_t w = (int64_t)blockIdx.x * WARPS + warp; w < tracks * parts; w += (int64_t)gridDim.x * WARPS)
-                batched_deposit_warp<T>(p.b.cfgs, p.task_cfg + t0, p.task_first + t0, p.task_prefix + t0,
-                                        (int)(t1 - t0), w / parts, p.xs, p.ys, (pair_t<T> *)p.dens[bi], p.counts,
-                                        lane, (int)(w % parts), parts);
+            const int nt = (int)(t1 - t0);
+            const int64_t nblk = batched_deposit_blocks(p.b.cfgs, p.task_cfg + t0, p.task_prefix + t0, nt, tracks);
+            for (int64_t vb = blockIdx.x; vb < nblk; vb += gridDim.x) {
+                __syncthreads();  // shared staging of the previous tile is done with
+                batched_deposit_block<T>(p.b.cfgs, p.task_cfg + t0, p.task_first + t0, p.task_prefix + t0, nt,
+                                         tracks, vb, p.xs, p.ys, (pair_t<T> *)p.dens[bi], p.counts, dep);
+            }
             if (!grid_barrier(barrier_ref(p.bar))) return;
         }
         BatchStepArgs<T> b = p.b;
@@ -399,10 +424,8 @@ static void launch_batched_step(const BatchLaunch &L, int bi, int bo, double *pa
 int batched_loop(const BatchLaunch &L, cudaStream_t st) { return batched_loop_stream(L, nullptr, st); }
 
 int batched_loop_stream(const BatchLaunch &L, const pic_batch_stream *B, cudaStream_t st) {
-    constexpr int WARPS = 8;
     unsigned int *counters = B ? nullptr : reinterpret_cast<unsigned int *>(L.workspace);
     double *partials = B ? nullptr : partials_of(L);
-    const int sms = sm_count();
     if (L.n_steps > 0 && !B) {
         int rc = L.dtype == PIC_F64 ? prep_table<double>(L, st) : prep_table<float>(L, st);
         if (rc) return rc;
@@ -413,16 +436,15 @@ int batched_loop_stream(const BatchLaunch &L, const pic_batch_stream *B, cudaStr
         const int64_t t0 = L.step_task_off[s], t1 = L.step_task_off[s + 1];
         const int64_t tracks = L.step_tracks[s];
         if (tracks > 0 && t1 > t0) {
-            const int parts = deposit_parts(tracks, sms);
-            const unsigned blocks = (unsigned)((tracks * parts + WARPS - 1) / WARPS);
+            const unsigned blocks = (unsigned)L.step_blocks[s];
             if (L.dtype == PIC_F64)
-                batched_deposit_kernel<double, WARPS><<<blocks, WARPS * 32, 0, st>>>(
+                batched_deposit_kernel<double><<<blocks, kDepThreads, 0, st>>>(
                     L.cfgs, L.task_cfg + t0, L.task_first + t0, L.task_prefix + t0, (int)(t1 - t0), tracks, L.xs,
-                    L.ys, (double2 *)L.dens[bi], L.counts, parts);
+                    L.ys, (double2 *)L.dens[bi], L.counts);
             else
-                batched_deposit_kernel<float, WARPS><<<blocks, WARPS * 32, 0, st>>>(
+                batched_deposit_kernel<float><<<blocks, kDepThreads, 0, st>>>(
                     L.cfgs, L.task_cfg + t0, L.task_first + t0, L.task_prefix + t0, (int)(t1 - t0), tracks, L.xs,
-                    L.ys, (float2 *)L.dens[bi], L.counts, parts);
+                    L.ys, (float2 *)L.dens[bi], L.counts);
             int rc = check_launch("batched_deposit_kernel");
             if (rc) return rc;
         }

@@ -241,12 +241,15 @@ static int check_batch_common(const pic_batch_launch *L) {
         return set_error(PIC_E_INVALID, "null pointer in the batch launch descriptor");
     int rc = check_fields(L->pos[0], L->neg[0], L->pos[1], L->neg[1]);
     if (rc) return rc;
-    if (!L->step_task_off || !L->step_tracks) return set_error(PIC_E_INVALID, "step task tables are null");
+    if (!L->step_task_off || !L->step_tracks || !L->step_blocks)
+        return set_error(PIC_E_INVALID, "step task tables are null");
     for (int64_t s = 0; s < L->n_steps; ++s) {
         if (L->step_task_off[s + 1] < L->step_task_off[s] || L->step_tracks[s] < 0)
             return set_error(PIC_E_INVALID, "step task offsets must be non-decreasing");
         if (L->step_tracks[s] > 0 && (!L->task_cfg || !L->task_first || !L->task_prefix || !L->xs || !L->ys))
             return set_error(PIC_E_INVALID, "track or task arrays are null");
+        if (L->step_tracks[s] > 0 && (L->step_blocks[s] < 1 || L->step_blocks[s] > 0x7fffffffLL))
+            return set_error(PIC_E_INVALID, "step_blocks must give each depositing step 1 .. 2^31-1 blocks");
     }
     return PIC_OK;
 }
@@ -272,11 +275,11 @@ extern "C" {
 
 const char *pic_last_error(void) { return g_last_error.c_str(); }
 
-// The Python binding mirrors pic_grid field by field (ABI 4: 5 int64, 14
+// The Python binding mirrors pic_grid field by field (ABI 5: 5 int64, 14
 // double, 9 int32, padded to 8 bytes).
 static_assert(sizeof(pic_grid) == 192, "pic_grid layout changed: bump pic_abi_version and the bindings");
 
-int pic_abi_version(void) { return 4; }
+int pic_abi_version(void) { return 5; }
 
 int64_t pic_kpitch(int64_t nzb) { return (nzb + 7) / 8 * 8; }
 

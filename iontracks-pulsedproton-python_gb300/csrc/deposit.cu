@@ -12,13 +12,18 @@
 //
 // The deposition is laid out [no_xy][dens_pitch(no_xy)] pairs (G * density,
 // G * the density of the four lateral neighbours; rows padded to 4 pairs).
-// One to eight warps per track (more when the step has few tracks), splitting
-// the box's rows. Lanes own stencil columns j; row factors are computed 32
-// rows at a time, one row per lane, and broadcast by shuffle. Each cell's pair
-// is added with one vector atomic: tracks overlap, and the L2 resolves the
-// collisions. The offset (i - x) is formed in float64 from the float64 track
-// centre before it is rounded, so the Gaussian is not shifted by the float32
-// spacing of x (up to 6e-5 voxel at x ~ 1000).
+// Two forms. Per track (large grids, tracks spread over many cells): one to
+// eight warps per track (more when the step has few tracks), splitting the
+// box's rows. Lanes own stencil columns j; row factors are computed 32 rows at
+// a time, one row per lane, and broadcast by shuffle. Each cell's pair is
+// added with one vector atomic: tracks overlap, and the L2 resolves the
+// collisions. Per tile (small grids, where hundreds of tracks a step pile onto
+// the same cells and those atomics serialise): a block sums every track that
+// reaches its 64 x 64 tile as sums of outer products of the tracks' row and
+// column factors, in registers, and adds each cell once per part
+// (deposit_tile in pic_deposit.cuh). In both, the offset (i - x) is formed
+// from the float64 track centre before it is rounded, so the Gaussian is not
+// shifted by the float32 spacing of x (up to 6e-5 voxel at x ~ 1000).
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -43,9 +48,43 @@ __global__ void __launch_bounds__(WARPS * 32) deposit_kernel(const double *__res
 }
 
 
+// The tile form (pic_deposit.cuh): block b sums part b % parts of the tracks
+// into tile b / parts.
+template <typename T>
+__global__ void __launch_bounds__(kDepThreads) deposit_tile_kernel(const double *__restrict__ xs,
+                                                                   const double *__restrict__ ys, int64_t m,
+                                                                   pair_t<T> *__restrict__ dens,
+                                                                   uint32_t *__restrict__ counts, int64_t n,
+                                                                   int64_t dp, double cut, T h2b2, T gfac, int parts) {
+    __shared__ DepTileShared<T> sh;
+    const int64_t tile = blockIdx.x / parts;
+    const int part = (int)(blockIdx.x % parts);
+    deposit_tile<T>(xs, ys, m * part / parts, m * (part + 1) / parts, n, dp, cut, h2b2, gfac, dens, counts, tile,
+                    sh);
+}
+
+// Track-tile pairs a step's deposition may scan in the tile form: beyond it
+// (a large grid) the per-track form, whose atomics then spread over many
+// cells, is cheaper than every tile scanning every track.
+constexpr int64_t kDepTileScanMax = 1000000;
+
 int launch_deposit(const pic_grid *g, const double *xs, const double *ys, int64_t m, void *dens, uint32_t *counts,
                    cudaStream_t st) {
     if (m <= 0) return PIC_OK;
+    const int64_t tiles = deposit_tiles(g->no_xy);
+    if (tiles * m <= kDepTileScanMax) {
+        const int parts = deposit_tile_parts(m);
+        const unsigned blocks = (unsigned)(tiles * parts);
+        if (g->dtype == PIC_F64)
+            deposit_tile_kernel<double><<<blocks, kDepThreads, 0, st>>>(
+                xs, ys, m, (double2 *)dens, counts, g->no_xy, dens_pitch(g->no_xy), g->cutoff_voxels,
+                g->h2_over_b2, g->gaussian_factor, parts);
+        else
+            deposit_tile_kernel<float><<<blocks, kDepThreads, 0, st>>>(
+                xs, ys, m, (float2 *)dens, counts, g->no_xy, dens_pitch(g->no_xy), g->cutoff_voxels,
+                (float)g->h2_over_b2, (float)g->gaussian_factor, parts);
+        return check_launch("deposit_tile_kernel");
+    }
     constexpr int WARPS = 8;
     const int parts = deposit_parts(m, sm_count());
     const int per_block = WARPS / parts;

@@ -69,7 +69,8 @@ def test_deposition_tasks_of_every_global_step():
     rng = np.random.default_rng(9)
     for _ in range(50):
         offsets, totals, base = _ragged_schedules(rng, int(rng.integers(1, 8)))
-        sto, stt, cfg, first, prefix = b._task_tables(offsets, totals, base)
+        sizes = rng.integers(3, 300, size=len(totals))
+        sto, stt, cfg, first, prefix, blocks = b._task_tables(offsets, totals, base, sizes)
         assert len(sto) == max(totals) + 1 and sto[0] == 0 and sto[-1] == len(cfg)
         for s in range(max(totals)):
             want = [(c, base[c] + offsets[c][s], offsets[c][s + 1] - offsets[c][s])
@@ -78,6 +79,8 @@ def test_deposition_tasks_of_every_global_step():
             assert [(cfg[t], first[t]) for t in got] == [(c, f) for c, f, _ in want]
             assert [prefix[t] for t in got] == list(np.cumsum([0] + [m for _, _, m in want])[:-1])
             assert stt[s] == sum(m for _, _, m in want)
+            tiles = lambda n: (-(-int(n) // 64)) ** 2  # noqa: E731
+            assert blocks[s] == sum(tiles(sizes[c]) * min(32, max(1, -(-m // 32))) for c, _, m in want)
 
 
 def test_work_tables_cover_each_active_grid_once():

@@ -57,9 +57,9 @@ def test_binding_covers_the_header(lib):
 
 
 def test_host_only_calls_without_a_gpu(lib):
-    assert lib.pic_abi_version() == 4
+    assert lib.pic_abi_version() == 5
     native = __import__("importlib").import_module(pkg().__name__ + "._native")
-    assert native.ABI_VERSION == 4
+    assert native.ABI_VERSION == 5
     assert ctypes.sizeof(native.PicGrid) == 192  # 5 int64, 14 double, 9 int32, padded to 8
     assert lib.pic_kpitch(406) == 408
     assert lib.pic_kpitch(408) == 408
