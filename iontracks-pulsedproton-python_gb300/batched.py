@@ -18,6 +18,7 @@ from a fixed meta-seed.
 
 from __future__ import annotations
 
+import copy
 import ctypes
 import warnings
 from time import perf_counter
@@ -281,6 +282,7 @@ def run_batched_b200(
     persistent: bool = False,
     solo_grids: int = SOLO_MAX_GRIDS,
     variant: str = "auto",
+    escalate: bool = True,
 ):
     """Simulate every configuration and return their Results, in order.
 
@@ -300,6 +302,9 @@ def run_batched_b200(
     queue), or "auto" (the flat step: over the whole 64-grid sweep the streaming
     step measured slower, 0.99 against 0.81 s of device time, although its
     launch in the 64-grid phase alone is the faster, 298 against 331 us).
+    ``escalate``: a float32 configuration whose tallies come back non-finite
+    is run again alone with float64 fields from the same generator state
+    (run_simulation_b200's ``escalate``), and that Result takes its place.
     """
     import torch
 
@@ -332,6 +337,7 @@ def run_batched_b200(
     # reference); the track centres are drawn later, chunk by chunk, while the
     # device runs the previous chunk (feeder.py)
     rngs = rngs if rngs is not None else [np.random.default_rng(c.seed) for c in configs]
+    rng_start = [copy.deepcopy(r.bit_generator.state) for r in rngs] if (escalate and dtype == "float32") else None
     offsets, samplers = [], []
     track_base = []
     base = 0
@@ -577,5 +583,15 @@ def run_batched_b200(
             p = q = np.zeros((0, 0, 0))
         res = diag.build_result(cfg, time_s, f_t, ks, p, q)
         res.loop_elapsed_s = elapsed
+        res.fields_dtype = dtype
+        rows = tally_h[tally_off[c] : tally_off[c] + totals[c]]
+        if rng_start is not None and not np.isfinite(rows).all():
+            # float32 fields could not follow this configuration: alone, same
+            # tracks, float64
+            rngs[c].bit_generator.state = rng_start[c]
+            from .solver_b200 import run_simulation_b200
+
+            res = run_simulation_b200(cfg, rng=rngs[c], progress=False, return_fields=return_fields,
+                                      dtype="float64", alpha_cm3_s=alpha_cm3_s, escalate=False)
         results.append(res)
     return results

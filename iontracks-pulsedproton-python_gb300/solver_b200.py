@@ -28,6 +28,7 @@ raises.
 
 from __future__ import annotations
 
+import copy
 from time import perf_counter
 from typing import Optional
 
@@ -72,6 +73,7 @@ def run_simulation_b200(
     shape: Optional[dict] = None,
     use_graphs: Optional[bool] = None,
     tune: bool = False,
+    escalate: bool = True,
 ):
     """Simulate a pulse train on one GB300 and return the reference's Result.
 
@@ -88,6 +90,15 @@ def run_simulation_b200(
     the same per-step track counts, so a pulse's chunks replay for every
     pulse); by default graphs are used for grids under 30 M voxels, where
     launch overhead is a visible part of a step.
+
+    ``escalate`` (float32 runs): when the run's tallies come back non-finite,
+    it is run again from the same generator state with float64 fields, and
+    that Result is returned. Near the explicit scheme's stability limit for
+    recombination (very high dose rates at low fields) an unstable mode grows
+    by a few per cent a step during the pulse: float64 round-off never lets it
+    matter, float32 round-off does, and the float32 run overflows. A
+    configuration that diverges in float64 too (as in the reference) stays
+    non-finite. ``Result.fields_dtype`` names the fields the result came from.
     """
     if dtype not in ("float32", "float64"):
         raise ValueError(f"dtype must be 'float32' or 'float64', got {dtype!r}")
@@ -96,6 +107,7 @@ def run_simulation_b200(
     total = int(config.total_time_steps)
     last_step = total if max_steps is None else max(0, min(total, int(max_steps)))
     rng = rng if rng is not None else np.random.default_rng(config.seed)
+    rng_start = copy.deepcopy(rng.bit_generator.state) if (escalate and dtype == "float32") else None
     schedule = build_track_schedule(config, rng)
     sampler = TrackSampler(rng, config.mid_xy, config.sampling_radius, config.no_xy)
     pulse_steps = int(config.pulse_time_steps)
@@ -175,8 +187,17 @@ def run_simulation_b200(
     else:
         pos, neg = np.zeros((0, 0, 0)), np.zeros((0, 0, 0))
     result = diagnostics.build_result(config, time_s, f_t, ks, pos, neg)
+    result.fields_dtype = dtype
     if max_wall_s is not None or max_steps is not None:
         result.steps_completed = steps_done
         result.loop_elapsed_s = loop_elapsed_s
     eng.close()
+    if rng_start is not None and not np.isfinite(tallies).all():
+        # float32 fields could not follow this configuration: run it again,
+        # same tracks, in float64
+        rng.bit_generator.state = rng_start
+        wide = None if not shape else {k: v for k, v in shape.items() if k != "variant"}
+        return run_simulation_b200(config, rng=rng, progress=progress, max_wall_s=max_wall_s, max_steps=max_steps,
+                                   return_fields=return_fields, dtype="float64", alpha_cm3_s=alpha_cm3_s,
+                                   chunk_steps=chunk_steps, shape=wide, use_graphs=use_graphs, escalate=False)
     return result

@@ -336,3 +336,25 @@ def test_stream_batched_matches_the_oracle_on_sweep_grids(oracle):
         ref = oracle.run(cfg, mode="batched", threads=8, keep_fields=False)
         np.testing.assert_array_equal(got.track_density_xy, ref["track_density_xy"])
         assert abs(got.ks - ref["ks"]) <= KS_ABS
+
+
+@pytest.mark.gpu
+def test_a_configuration_float32_cannot_follow_is_run_again_in_float64():
+    """Sweep configuration 6 (32.6 V over 0.3 cm at 65 Gy/s, k_s 32.7) sits
+    near the explicit scheme's recombination stability limit: an unstable mode
+    grows a few per cent a step during the pulse, and float32 round-off makes it
+    overflow where float64 round-off does not. The float32 call detects the
+    non-finite tallies and returns the float64 run of the same tracks, within
+    1e-5 of the oracle's k_s; a well-conditioned configuration stays float32."""
+    from goldens import histogram_sha256, oracle_fixture
+
+    fx = oracle_fixture("oracle_sweep64")["configs"]
+    cfgs = pkg().saturation_sweep_configs()
+    hard = pkg().run_simulation_b200(cfgs[6], progress=False, return_fields=False)
+    assert hard.fields_dtype == "float64"
+    assert abs(hard.ks - fx[6]["ks"]) <= KS_ABS
+    assert histogram_sha256(hard.track_density_xy) == fx[6]["track_sha256"]
+    easy = pkg().run_simulation_b200(cfgs[0], progress=False, return_fields=False)
+    assert easy.fields_dtype == "float32" and abs(easy.ks - fx[0]["ks"]) <= KS_ABS
+    nan = pkg().run_simulation_b200(cfgs[27], progress=False, return_fields=False)
+    assert nan.fields_dtype == "float64" and not np.isfinite(nan.ks)  # as in the reference
