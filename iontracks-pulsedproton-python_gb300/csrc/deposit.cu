@@ -67,12 +67,19 @@ __global__ void __launch_bounds__(kDepThreads) deposit_tile_kernel(const double 
 // (a large grid) the per-track form, whose atomics then spread over many
 // cells, is cheaper than every tile scanning every track.
 constexpr int64_t kDepTileScanMax = 1000000;
+// ... and only when a step's tiles and parts give enough blocks to fill the
+// GPU: a single small grid with a few hundred tracks is faster with the
+// per-track warps spread over every SM (a 48 x 48 grid's whole run: 21 ms
+// per track, 31 ms in tiles); the batched step always deposits in tiles,
+// where every grid's tiles together fill the GPU.
+constexpr int64_t kDepTileMinBlocks = 1024;
 
 int launch_deposit(const pic_grid *g, const double *xs, const double *ys, int64_t m, void *dens, uint32_t *counts,
                    cudaStream_t st) {
     if (m <= 0) return PIC_OK;
     const int64_t tiles = deposit_tiles(g->no_xy);
-    if (tiles * m <= kDepTileScanMax) {
+    const int parts_est = deposit_tile_parts(m);
+    if (tiles * m <= kDepTileScanMax && tiles * parts_est >= kDepTileMinBlocks) {
         const int parts = deposit_tile_parts(m);
         const unsigned blocks = (unsigned)(tiles * parts);
         if (g->dtype == PIC_F64)
