@@ -166,7 +166,7 @@ __global__ void __launch_bounds__((kAdjStreamWarps + 1) * 32, 1) adjoint_stream_
         const float2 NLT = make_float2(a.n_lat, a.n_lat), NCN = make_float2(a.n_cen, a.n_cen);
         const float2 AD = make_float2(a.a, a.a), CPOS = make_float2(a.c_pos, a.c_pos);
         const float2 CNEG = make_float2(a.c_neg, a.c_neg), HALF = make_float2(0.5f, 0.5f);
-        const float2 M2 = make_float2(-2.f, -2.f), M4 = make_float2(-4.f, -4.f);
+        const float2 M2 = make_float2(-2.f, -2.f), M6 = make_float2(-6.f, -6.f);
         long long g = 0;
         for (int w = blockIdx.x; w < a.n_items; w += gridDim.x) {
             const int u = w / a.jt, t = w - u * a.jt;
@@ -309,45 +309,60 @@ __global__ void __launch_bounds__((kAdjStreamWarps + 1) * 32, 1) adjoint_stream_
                             const int64_t rcol = (int64_t)ri * n + rj;
                             st4(a.lp_out + rcol * kp + k0, RP);
                             st4(a.ln_out + rcol * kp + k0, RN);
+                            if (tgt < 2) {
+                                // the ring column's u~ enters the lateral sum of this
+                                // interior column: its share of dR/ds (summed by parts
+                                // below, the ring columns are no centres of their own)
+                                const float4 UP = lds4(Sr + 2 * spec + row * kp + k0);
+                                const float4 UN = lds4(Sr + 3 * spec + row * kp + k0);
+                                float gp = 0.f, gn = 0.f;
+#pragma unroll
+                                for (int e = 0; e < 4; ++e) {
+                                    gp = fmaf(comp(UP, e), comp(MP, e), gp);
+                                    gn = fmaf(comp(UN, e), comp(MN, e), gn);
+                                }
+                                G0.x += gp;
+                                G2.x += gn;
+                            }
                         }
                     }
 
-                    // derivative sums of this column's outputs (mu is zero where
-                    // k is not valid, so no masks)
-                    const float dkm = (k0 - 1 >= a.nze && k0 - 1 < a.gap_end) ? dc : 0.f;
-                    const float dkp = (k0 + 4 >= a.nze && k0 + 4 < a.gap_end) ? dc : 0.f;
-                    const float pkm = k0 >= 1 ? Sc[2 * spec + o - 1] + dkm : 0.f;
-                    const float nkm = k0 >= 1 ? Sc[3 * spec + o - 1] + dkm : 0.f;
-                    const float pkp = k0 + 4 < kp ? Sc[2 * spec + o + 4] + dkp : 0.f;
-                    const float nkp = k0 + 4 < kp ? Sc[3 * spec + o + 4] + dkp : 0.f;
-                    const float4 S0 = lds4(Sm + 2 * spec + o), T0 = lds4(Sm + 3 * spec + o);
-                    const float4 S1 = lds4(Sp + 2 * spec + o), T1 = lds4(Sp + 3 * spec + o);
-                    const float4 S2 = lds4(Sc + 2 * spec + o - kp), T2 = lds4(Sc + 3 * spec + o - kp);
-                    const float4 S3 = lds4(Sc + 2 * spec + o + kp), T3 = lds4(Sc + 3 * spec + o + kp);
+                    // derivative sums, summed by parts: sum_v mu(v) D u(v) =
+                    // sum_w u(w) D' mu(w) over the voxels w this column holds,
+                    // with D' the transposed difference (the 7-point Laplacian is
+                    // its own transpose; the z differences swap their ends). mu
+                    // is zero off the interior columns and valid k, u is zero on
+                    // the z end planes and padding, so the only terms beyond
+                    // these columns' voxels are the ring columns' u in their
+                    // interior neighbours' lateral sums, added with the ring
+                    // writes above. The lateral neighbours enter as the raw state
+                    // plus this column's pair of neighbour deposition (dl), a
+                    // local term; the z neighbours and the centre carry their own
+                    // column's deposition (u~). Every mu value needed is already
+                    // loaded for lambda; no neighbour of the state is read.
                     const float2 DLl = make_float2(g4[0] ? dl : 0.f, g4[1] ? dl : 0.f);
                     const float2 DLh = make_float2(g4[2] ? dl : 0.f, g4[3] ? dl : 0.f);
-                    const float2 SPl = add2(add2(add2(add2(lo2(S0), lo2(S1)), lo2(S2)), lo2(S3)), DLl);
-                    const float2 SPh = add2(add2(add2(add2(hi2(S0), hi2(S1)), hi2(S2)), hi2(S3)), DLh);
-                    const float2 SNl = add2(add2(add2(add2(lo2(T0), lo2(T1)), lo2(T2)), lo2(T3)), DLl);
-                    const float2 SNh = add2(add2(add2(add2(hi2(T0), hi2(T1)), hi2(T2)), hi2(T3)), DLh);
-                    const float2 pdl = make_float2(pkm, Pl.x), pdh = make_float2(Pl.y, Ph.x);
-                    const float2 pul = make_float2(Pl.y, Ph.x), puh = make_float2(Ph.y, pkp);
-                    const float2 ndl = make_float2(nkm, Nl.x), ndh = make_float2(Nl.y, Nh.x);
-                    const float2 nul = make_float2(Nl.y, Nh.x), nuh = make_float2(Nh.y, nkp);
-                    // z second difference, 7-point Laplacian, Courant derivative
-                    const float2 pz2l = fma2(M2, Pl, add2(pdl, pul)), pz2h = fma2(M2, Ph, add2(pdh, puh));
-                    const float2 nz2l = fma2(M2, Nl, add2(ndl, nul)), nz2h = fma2(M2, Nh, add2(ndh, nuh));
-                    const float2 plapl = add2(fma2(M4, Pl, SPl), pz2l), plaph = add2(fma2(M4, Ph, SPh), pz2h);
-                    const float2 nlapl = add2(fma2(M4, Nl, SNl), nz2l), nlaph = add2(fma2(M4, Nh, SNh), nz2h);
-                    const float2 pcl = fma2(CPOS, pz2l, mul2(HALF, sub2(pdl, pul)));
-                    const float2 pch = fma2(CPOS, pz2h, mul2(HALF, sub2(pdh, puh)));
-                    const float2 ncl = fma2(CNEG, nz2l, mul2(HALF, sub2(nul, ndl)));
-                    const float2 nch = fma2(CNEG, nz2h, mul2(HALF, sub2(nuh, ndh)));
+                    const float2 zsp_l = add2(mpu_l, mpd_l), zsp_h = add2(mpu_h, mpd_h);
+                    const float2 zsn_l = add2(mnu_l, mnd_l), zsn_h = add2(mnu_h, mnd_h);
+                    // z neighbours and centre of the Laplacian of mu: z sum - 6 mu
+                    const float2 plm_l = fma2(M6, MPl, zsp_l), plm_h = fma2(M6, MPh, zsp_h);
+                    const float2 nlm_l = fma2(M6, MNl, zsn_l), nlm_h = fma2(M6, MNh, zsn_h);
+                    // transposed Courant derivative: c (mu[w+z] + mu[w-z] - 2 mu[w]) plus
+                    // (mu[w+z] - mu[w-z]) / 2 (positive) or its negative (negative,
+                    // which drifts the other way)
+                    const float2 pcm_l = fma2(CPOS, fma2(M2, MPl, zsp_l), mul2(HALF, sub2(mpu_l, mpd_l)));
+                    const float2 pcm_h = fma2(CPOS, fma2(M2, MPh, zsp_h), mul2(HALF, sub2(mpu_h, mpd_h)));
+                    const float2 ncm_l = fma2(CNEG, fma2(M2, MNl, zsn_l), mul2(HALF, sub2(mnd_l, mnu_l)));
+                    const float2 ncm_h = fma2(CNEG, fma2(M2, MNh, zsn_h), mul2(HALF, sub2(mnd_h, mnu_h)));
                     const float2 pnl = mul2(Pl, Nl), pnh = mul2(Ph, Nh);
-                    G0 = fma2(MPh, plaph, fma2(MPl, plapl, G0));
-                    G1 = fma2(MPh, pch, fma2(MPl, pcl, G1));
-                    G2 = fma2(MNh, nlaph, fma2(MNl, nlapl, G2));
-                    G3 = fma2(MNh, nch, fma2(MNl, ncl, G3));
+                    // dR/ds: raw u against the lateral sum of mu (by parts), u~
+                    // against its z neighbours and centre, mu against dl (local)
+                    G0 = fma2(lo2(P0), LPl, fma2(Pl, plm_l, fma2(MPl, DLl, G0)));
+                    G0 = fma2(hi2(P0), LPh, fma2(Ph, plm_h, fma2(MPh, DLh, G0)));
+                    G1 = fma2(Ph, pcm_h, fma2(Pl, pcm_l, G1));
+                    G2 = fma2(lo2(N0), LNl, fma2(Nl, nlm_l, fma2(MNl, DLl, G2)));
+                    G2 = fma2(hi2(N0), LNh, fma2(Nh, nlm_h, fma2(MNh, DLh, G2)));
+                    G3 = fma2(Nh, ncm_h, fma2(Nl, ncm_l, G3));
                     G4 = fma2(neg2(Ssh), pnh, fma2(neg2(Ssl), pnl, G4));
                     G4 = add2(G4, make_float2(sc[0] ? pnl.x : 0.f, sc[1] ? pnl.y : 0.f));
                     G4 = add2(G4, make_float2(sc[2] ? pnh.x : 0.f, sc[3] ? pnh.y : 0.f));
