@@ -20,6 +20,7 @@ from __future__ import annotations
 
 import copy
 import ctypes
+import threading
 import warnings
 from time import perf_counter
 from typing import Optional, Sequence
@@ -474,11 +475,59 @@ def run_batched_b200(
             out.append((samplers[c], int(b - a), int(track_base[c] + a)))
         return out
 
+    # float64 re-runs of configurations whose float32 tallies go non-finite:
+    # after every chunk the tallies are copied back on a side stream; a grid
+    # found diverged is re-run at once from its starting generator state on
+    # a stream of its own, beside the rest of the batch (its float64 kernels
+    # are bound by the FP64 units, the batch by memory and latency)
+    from .solver_b200 import run_simulation_b200
+
+    redo, redo_threads = {}, {}
+
+    def redo_one(c):
+        bg = type(rngs[c].bit_generator)()
+        bg.state = rng_start[c]
+        try:
+            with torch.cuda.device(dev), torch.cuda.stream(torch.cuda.Stream(device=dev)):
+                redo[c] = run_simulation_b200(configs[c], rng=np.random.Generator(bg), progress=False,
+                                              return_fields=return_fields, dtype="float64",
+                                              alpha_cm3_s=alpha_cm3_s, escalate=False)
+        except BaseException as exc:  # re-raised by the caller's thread
+            redo[c] = exc
+
+    watch = rng_start is not None and bool(chunks)
+    if watch:
+        tally_pin = torch.empty(tuple(tally.shape), dtype=tally.dtype, pin_memory=True)
+        side = torch.cuda.Stream(device=dev)
+        copy_ev = None
+
+    def watch_tallies(final=False):
+        nonlocal copy_ev
+        if copy_ev is not None and (final or copy_ev.query()):
+            copy_ev.synchronize()
+            host = tally_pin.numpy()
+            for c in range(n_cfg):
+                if c not in redo_threads and not np.isfinite(host[tally_off[c] : tally_off[c] + totals[c]]).all():
+                    th = threading.Thread(target=redo_one, args=(c,), daemon=True)
+                    redo_threads[c] = th
+                    th.start()
+            copy_ev = None
+        if copy_ev is None and not final:
+            done = torch.cuda.Event()
+            done.record(torch.cuda.current_stream(dev))
+            side.wait_event(done)
+            with torch.cuda.stream(side):
+                tally_pin.copy_(tally, non_blocking=True)
+                copy_ev = torch.cuda.Event()
+                copy_ev.record(side)
+
     feeder = TrackFeeder(torch, dev, max((sum(n for _, n, _ in jobs_of(c0, c1)) for c0, c1, _ in chunks), default=1))
     t0 = perf_counter()
     try:
         pending = feeder.submit(jobs_of(*chunks[0][:2])) if chunks else None
         for k, (c0, c1, tab) in enumerate(chunks):
+            if watch and k > 0:
+                watch_tallies()
             feeder.upload(pending, xs_dev, ys_dev)
             # draw the next chunk's tracks while the device runs this one
             pending = feeder.submit(jobs_of(*chunks[k + 1][:2])) if k + 1 < len(chunks) else None
@@ -549,6 +598,8 @@ def run_batched_b200(
                                    "results are invalid")
     finally:
         feeder.close()
+        for th in redo_threads.values():
+            th.join()
         if solo_graphs:  # an exception left graphs behind: let them finish, then free them
             try:
                 torch.cuda.synchronize(dev)
@@ -586,12 +637,13 @@ def run_batched_b200(
         res.fields_dtype = dtype
         rows = tally_h[tally_off[c] : tally_off[c] + totals[c]]
         if rng_start is not None and not np.isfinite(rows).all():
-            # float32 fields could not follow this configuration: alone, same
-            # tracks, float64
-            rngs[c].bit_generator.state = rng_start[c]
-            from .solver_b200 import run_simulation_b200
-
-            res = run_simulation_b200(cfg, rng=rngs[c], progress=False, return_fields=return_fields,
-                                      dtype="float64", alpha_cm3_s=alpha_cm3_s, escalate=False)
+            # float32 fields could not follow this configuration: its float64
+            # run of the same tracks (started during the batch when the
+            # divergence showed before the last chunk)
+            if c not in redo:
+                redo_one(c)
+            if isinstance(redo[c], BaseException):
+                raise redo[c]
+            res = redo[c]
         results.append(res)
     return results
