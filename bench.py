@@ -593,7 +593,7 @@ def run_gb300(args):
             torch.cuda.empty_cache()
             sweep = sweep_measure()
             sweep["workload"] = SWEEP_DESC.format(n=sweep.pop("n_total"))
-            adjoint = adjoint_measure(warmup=3, reps=3)
+            adjoint = adjoint_measure(warmup=3, reps=5)
         else:
             sweep = adjoint = {"skipped": "measured by the single-GPU run only"}
 

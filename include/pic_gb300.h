@@ -78,7 +78,26 @@ typedef struct pic_grid {
      * AUTO: STREAM for float32 grids with no_xy >= 4 and no_xy^2 * kpitch >=
      * 2^24 cells, FLAT otherwise; STREAM on a float64 grid is refused. */
     int32_t adjoint_variant;
+    /* Deposition form (PIC_DEPOSIT_*). */
+    int32_t deposit_variant;
 } pic_grid;
+
+/* Deposition forms. TRACKS: one to eight warps per track, each cell's pair
+ * added with a vector atomic (any call). BINNED: a binning launch lists each
+ * track in the 62 x 62-cell tiles its box meets, then one block per tile sums
+ * its tracks' separable Gaussians as outer products in ascending track order
+ * and stores each cell once (no atomics on the pairs; two runs give identical
+ * pairs). It needs the track lists of the step workspace, so only the calls
+ * that take one use it (pic_run_segment, the graph capture, the gradient
+ * drivers), for no_xy <= 4096 and cutoff_voxels < 31.5 (truncation boxes of
+ * at most 64 cells); elsewhere BINNED is refused. AUTO: BINNED
+ * where it can run and the grid has at least two tiles per SM (no_xy >= 1055
+ * on 152 SMs); otherwise TRACKS, or on small grids
+ * whose steps bring many tracks a scan-tile form (every block scans the
+ * step's tracks; one vector atomic per cell and block). */
+#define PIC_DEPOSIT_AUTO 0
+#define PIC_DEPOSIT_TRACKS 1
+#define PIC_DEPOSIT_BINNED 2
 
 /* Fused-step kernels. FLAT: one thread per four k of a column, neighbours
  * through L1/L2, any grid and either field type. STREAM: float32 only; whole
@@ -109,9 +128,13 @@ int64_t pic_dens_pitch(int64_t no_xy);
 int pic_device_info(int32_t *sm_count, int64_t *total_bytes, int32_t *cc_major, int32_t *cc_minor);
 
 /* Bytes of device scratch the fused step needs for this grid (per-block
- * tally partials, a completion counter and a status word). The caller
- * allocates it once, zero-filled, and passes it to pic_step /
- * pic_run_segment. */
+ * tally partials, a completion counter, a status word and, where the
+ * binned deposition can run, its per-tile track lists and the boxes and
+ * Gaussian factors of up to 16384 tracks: about 14 MB for a 1068 x 1068
+ * float32 grid). The caller allocates it once, zero-filled, and passes it
+ * to pic_step / pic_run_segment; every call leaves its counters at zero again.
+ * A workspace of the fixed part alone (ABI 5's size) is still accepted: the
+ * deposition then runs without the binned form. */
 int pic_step_workspace_bytes(const pic_grid *g, int64_t *bytes);
 
 /* Reads (and with reset != 0 clears) the status word a kernel sets in the

@@ -23,8 +23,11 @@ PIC_WALL_REFLECTING = 1
 PIC_VARIANT_AUTO = 0
 PIC_VARIANT_FLAT = 1
 PIC_VARIANT_STREAM = 2
+PIC_DEPOSIT_AUTO = 0
+PIC_DEPOSIT_TRACKS = 1
+PIC_DEPOSIT_BINNED = 2
 # pic_abi_version() of the library these structures mirror
-ABI_VERSION = 5
+ABI_VERSION = 6
 
 _LIB_PATH = Path(__file__).resolve().parent / "_build" / "libpic_gb300.so"
 _lock = threading.Lock()
@@ -64,6 +67,7 @@ class PicGrid(ctypes.Structure):
         ("ctas_per_sm", ctypes.c_int32),
         ("steps_per_launch", ctypes.c_int32),
         ("adjoint_variant", ctypes.c_int32),
+        ("deposit_variant", ctypes.c_int32),
     ]
 
 

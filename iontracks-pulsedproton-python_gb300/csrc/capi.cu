@@ -164,6 +164,9 @@ static int check_grid(const pic_grid *g) {
         return set_error(PIC_E_INVALID, "adjoint_variant must be PIC_VARIANT_AUTO, _FLAT or _STREAM");
     if (g->adjoint_variant == PIC_VARIANT_STREAM && g->dtype != PIC_F32)
         return set_error(PIC_E_INVALID, "the stream adjoint variant supports float32 fields only");
+    if (g->deposit_variant != PIC_DEPOSIT_AUTO && g->deposit_variant != PIC_DEPOSIT_TRACKS &&
+        g->deposit_variant != PIC_DEPOSIT_BINNED)
+        return set_error(PIC_E_INVALID, "deposit_variant must be PIC_DEPOSIT_AUTO, _TRACKS or _BINNED");
     ScoreTest t;
     return score_test(g, &t);
 }
@@ -180,7 +183,7 @@ static int check_fields(const void *a, const void *b, const void *c, const void 
 static int run_loop(const pic_grid *g, void *pos0, void *neg0, void *pos1, void *neg1, int64_t parity,
                     int64_t n_steps, const double *xs, const double *ys, const int64_t *off, void *dens0,
                     void *dens1, int64_t dens_parity, uint32_t *counts, double *tally, void *ws,
-                    cudaStream_t st) {
+                    int64_t ws_bytes, cudaStream_t st) {
     void *pos[2] = {pos0, pos1}, *neg[2] = {neg0, neg1}, *dens[2] = {dens0, dens1};
     pic_grid r = *g;
     int rc0 = resolve_shape(&r);
@@ -204,7 +207,7 @@ static int run_loop(const pic_grid *g, void *pos0, void *neg0, void *pos1, void 
         const int di = (int)((dens_parity + s) & 1);
         const int64_t m = off[s + 1] - off[s];
         if (m > 0) {
-            int rc = launch_deposit(g, xs + off[s], ys + off[s], m, dens[di], counts, st);
+            int rc = launch_deposit(g, xs + off[s], ys + off[s], m, dens[di], counts, st, ws, ws_bytes);
             if (rc) return rc;
         }
         // The buffer step s+1 accumulates into was last written at step s-1.
@@ -277,9 +280,9 @@ const char *pic_last_error(void) { return g_last_error.c_str(); }
 
 // The Python binding mirrors pic_grid field by field (ABI 5: 5 int64, 14
 // double, 9 int32, padded to 8 bytes).
-static_assert(sizeof(pic_grid) == 192, "pic_grid layout changed: bump pic_abi_version and the bindings");
+static_assert(sizeof(pic_grid) == 200, "pic_grid layout changed: bump pic_abi_version and the bindings");
 
-int pic_abi_version(void) { return 5; }
+int pic_abi_version(void) { return 6; }
 
 int64_t pic_kpitch(int64_t nzb) { return (nzb + 7) / 8 * 8; }
 
@@ -306,7 +309,7 @@ int pic_step_workspace_bytes(const pic_grid *g, int64_t *bytes) {
     int rc = check_grid(g);
     if (rc) return rc;
     if (!bytes) return set_error(PIC_E_INVALID, "bytes is null");
-    *bytes = kWorkspaceBytes;
+    *bytes = kWorkspaceBytes + dep_bin_bytes(g);
     return PIC_OK;
 }
 
@@ -489,7 +492,9 @@ int pic_adjoint_forward(const pic_grid *g, void *pos0, void *neg0, void *pos1, v
         void *dens = nullptr;
         if (m > 0) {
             dens = D + (d++) * dslot * es;
-            if ((rc = launch_deposit(g, xs + track_offsets[s], ys + track_offsets[s], m, dens, counts, st))) return rc;
+            if ((rc = launch_deposit(g, xs + track_offsets[s], ys + track_offsets[s], m, dens, counts, st, workspace,
+                                     workspace_bytes)))
+                return rc;
         }
         rc = launch_step(g, pos[b], neg[b], pos[b ^ 1], neg[b ^ 1], dens, nullptr, tally + 4 * s, workspace, st);
         if (rc) return rc;
@@ -615,7 +620,8 @@ int pic_revolve_forward(const pic_grid *g, void *pos0, void *neg0, void *pos1, v
     if (!workspace || workspace_bytes < kWorkspaceBytes)
         return set_error(PIC_E_INVALID, "workspace too small (pic_step_workspace_bytes)");
     return revolve_forward(g, pos0, neg0, pos1, neg1, n_steps, xs, ys, track_offsets, dens, counts, tally, slots_pos,
-                           slots_neg, state_stride, n_slots, workspace, reinterpret_cast<cudaStream_t>(stream));
+                           slots_neg, state_stride, n_slots, workspace, workspace_bytes,
+                           reinterpret_cast<cudaStream_t>(stream));
 }
 
 int pic_revolve_backward(const pic_grid *g, void *slots_pos, void *slots_neg, int64_t state_stride, int64_t n_slots,
@@ -639,7 +645,7 @@ int pic_revolve_backward(const pic_grid *g, void *slots_pos, void *slots_neg, in
         return set_error(PIC_E_INVALID, "adjoint workspace too small (pic_adjoint_workspace_bytes)");
     return revolve_backward(g, slots_pos, slots_neg, state_stride, n_slots, n_steps, xs, ys, track_offsets, dens,
                             work_pos0, work_neg0, work_pos1, work_neg1, lam_pos0, lam_neg0, lam_pos1, lam_neg1, grad,
-                            workspace, adj_workspace, reinterpret_cast<cudaStream_t>(stream));
+                            workspace, workspace_bytes, adj_workspace, reinterpret_cast<cudaStream_t>(stream));
 }
 
 int pic_run_segment(const pic_grid *g, void *pos0, void *neg0, void *pos1, void *neg1, int64_t parity,
@@ -651,7 +657,7 @@ int pic_run_segment(const pic_grid *g, void *pos0, void *neg0, void *pos1, void 
                            workspace, workspace_bytes);
     if (rc) return rc;
     return run_loop(g, pos0, neg0, pos1, neg1, parity, n_steps, xs, ys, track_offsets, dens0, dens1, dens_parity,
-                    counts, tally, workspace, reinterpret_cast<cudaStream_t>(stream));
+                    counts, tally, workspace, workspace_bytes, reinterpret_cast<cudaStream_t>(stream));
 }
 
 int pic_graph_create(const pic_grid *g, void *pos0, void *neg0, void *pos1, void *neg1, int64_t parity,
@@ -678,7 +684,7 @@ int pic_graph_create(const pic_grid *g, void *pos0, void *neg0, void *pos1, void
         return set_cuda_error("cudaStreamBeginCapture", e);
     }
     rc = run_loop(g, pos0, neg0, pos1, neg1, parity, n_steps, xs, ys, track_offsets, dens0, dens1, dens_parity,
-                  counts, tally, workspace, st);
+                  counts, tally, workspace, workspace_bytes, st);
     e = cudaStreamEndCapture(st, &graph);
     if (own) cudaStreamDestroy(own);
     if (rc) {

@@ -138,8 +138,53 @@ int step_occupancy(int dtype, int *blocks_per_sm);
 
 int launch_step(const pic_grid *g, const void *pos_in, const void *neg_in, void *pos_out, void *neg_out,
                 const void *dens, void *dens_zero, double *tally, void *ws, cudaStream_t st);
+// The deposition of one step's m tracks into dens. ws / ws_bytes: the step
+// workspace when the caller has one (null otherwise); its track lists, behind
+// the fixed part, let the binned form run.
 int launch_deposit(const pic_grid *g, const double *xs, const double *ys, int64_t m, void *dens,
-                   uint32_t *counts, cudaStream_t st);
+                   uint32_t *counts, cudaStream_t st, void *ws = nullptr, int64_t ws_bytes = 0);
+
+// Binned tile deposition (deposit.cu): a binning launch evaluates each
+// track's Gaussian row and column factors once and lists the track in the
+// tiles of kBinOut x kBinOut cells its written box meets; then one block per
+// tile sums its tracks' outer products in a fixed order and stores each cell
+// once. Its scratch sits in the step workspace behind kWorkspaceBytes: a
+// count per tile (zero between steps; the tile's block clears it), kBinCap
+// track indices per tile (a tile with more scans every track), and the boxes
+// and factors of up to kBinGroup tracks (a step with more runs in groups).
+constexpr int kBinOut = 62;
+constexpr int kBinCap = 4096;
+constexpr int kBinGroup = 16384;
+constexpr int kBinBox = 64;               // factors kept per track and axis
+constexpr int64_t kBinMaxNoXy = 4096;     // largest grid with track lists
+// AUTO takes the binned form where a grid's tiles give at least this many
+// blocks per SM (no_xy >= 1055 on 152 SMs): on smaller grids the per-track
+// warps, spread over every SM, finish first (measured on GB300: 1068^2 with
+// 8 500 tracks a step 45 against 64 us; 608^2 with 2 700 even; 608^2 with
+// 27 000 and 208^2 with 300 slower in tiles)
+constexpr int kBinAutoTilesPerSm = 2;
+inline int64_t bin_tiles_per_side(int64_t n) { return (n + kBinOut - 1) / kBinOut; }
+inline int64_t bin_align(int64_t b) { return (b + 255) / 256 * 256; }
+inline int64_t bin_count_bytes(int64_t n) {
+    const int64_t t = bin_tiles_per_side(n);
+    return bin_align(t * t * 4);
+}
+inline int64_t bin_list_bytes(int64_t n) {
+    const int64_t t = bin_tiles_per_side(n);
+    return t * t * kBinCap * 4;
+}
+inline int64_t bin_box_bytes() { return bin_align((int64_t)kBinGroup * 8); }
+// A grid takes the binned form when its track lists fit (no_xy <= 4096) and
+// every truncation box, [ceil(c - cut), floor(c + cut)], spans at most
+// kBinBox cells (floor(2 cut) + 1 of them at most).
+inline bool bin_eligible(const pic_grid *g) {
+    return g->no_xy <= kBinMaxNoXy && g->cutoff_voxels > 0.0 && 2.0 * g->cutoff_voxels + 1.0 < (double)kBinBox;
+}
+inline int64_t dep_bin_bytes(const pic_grid *g) {
+    if (!bin_eligible(g)) return 0;
+    const int64_t es = g->dtype == PIC_F64 ? 8 : 4;
+    return bin_count_bytes(g->no_xy) + bin_list_bytes(g->no_xy) + bin_box_bytes() + (int64_t)kBinGroup * 2 * kBinBox * es;
+}
 using BatchLaunch = pic_batch_launch;
 int batched_workspace_bytes(int32_t n_blocks, int32_t n_cfgs, int64_t *bytes);
 int batched_loop(const BatchLaunch &L, cudaStream_t st);
@@ -192,12 +237,12 @@ int revolve_trace(int64_t n_steps, int64_t n_slots, int64_t *events, int64_t cap
 int revolve_forward(const pic_grid *g, void *pos0, void *neg0, void *pos1, void *neg1, int64_t n_steps,
                     const double *xs, const double *ys, const int64_t *off, void *dens, uint32_t *counts,
                     double *tally, void *slots_pos, void *slots_neg, int64_t state_stride, int64_t n_slots, void *ws,
-                    cudaStream_t st);
+                    int64_t ws_bytes, cudaStream_t st);
 int revolve_backward(const pic_grid *g, void *slots_pos, void *slots_neg, int64_t state_stride, int64_t n_slots,
                      int64_t n_steps, const double *xs, const double *ys, const int64_t *off, void *dens,
                      void *work_pos0, void *work_neg0, void *work_pos1, void *work_neg1, void *lam_pos0,
-                     void *lam_neg0, void *lam_pos1, void *lam_neg1, double *grad, void *ws, void *adj_ws,
-                     cudaStream_t st);
+                     void *lam_neg0, void *lam_pos1, void *lam_neg1, double *grad, void *ws, int64_t ws_bytes,
+                     void *adj_ws, cudaStream_t st);
 
 int selftest_waits(int32_t *barrier_status, int32_t *mbarrier_status, cudaStream_t st);
 

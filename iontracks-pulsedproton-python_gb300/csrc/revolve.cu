@@ -201,6 +201,7 @@ struct DeviceExecutor : Executor {
     const int64_t *off;
     void *dens;             // one step's deposition pairs (scratch)
     void *ws;               // step workspace
+    int64_t ws_bytes;
     void *lam[2][2];        // [buffer][species]
     int cur = 0;            // lambda_{s+1} is in lam[cur]
     void *adj_ws;
@@ -214,7 +215,7 @@ struct DeviceExecutor : Executor {
         if (m <= 0) return PIC_OK;
         cudaError_t e = cudaMemsetAsync(dens, 0, (size_t)(dslot * es), st);
         if (e != cudaSuccess) return set_cuda_error("cudaMemsetAsync(deposition scratch)", e);
-        int rc = launch_deposit(g, xs + off[s], ys + off[s], m, dens, nullptr, st);
+        int rc = launch_deposit(g, xs + off[s], ys + off[s], m, dens, nullptr, st, ws, ws_bytes);
         if (rc) return rc;
         *d = dens;
         return PIC_OK;
@@ -291,7 +292,7 @@ int revolve_trace(int64_t n_steps, int64_t n_slots, int64_t *events, int64_t cap
 int revolve_forward(const pic_grid *g, void *pos0, void *neg0, void *pos1, void *neg1, int64_t n_steps,
                     const double *xs, const double *ys, const int64_t *off, void *dens, uint32_t *counts,
                     double *tally, void *slots_pos, void *slots_neg, int64_t state_stride, int64_t n_slots, void *ws,
-                    cudaStream_t st) {
+                    int64_t ws_bytes, cudaStream_t st) {
     const int64_t es = g->dtype == PIC_F64 ? 8 : 4;
     const int64_t field = g->no_xy * g->no_xy * g->kpitch;
     const int64_t dslot = 2 * g->no_xy * dens_pitch(g->no_xy);
@@ -313,7 +314,7 @@ int revolve_forward(const pic_grid *g, void *pos0, void *neg0, void *pos1, void 
         if (m > 0) {
             cudaError_t e = cudaMemsetAsync(dens, 0, (size_t)(dslot * es), st);
             if (e != cudaSuccess) return set_cuda_error("cudaMemsetAsync(deposition scratch)", e);
-            int rc = launch_deposit(g, xs + off[s], ys + off[s], m, dens, counts, st);
+            int rc = launch_deposit(g, xs + off[s], ys + off[s], m, dens, counts, st, ws, ws_bytes);
             if (rc) return rc;
             d = dens;
         }
@@ -326,8 +327,8 @@ int revolve_forward(const pic_grid *g, void *pos0, void *neg0, void *pos1, void 
 int revolve_backward(const pic_grid *g, void *slots_pos, void *slots_neg, int64_t state_stride, int64_t n_slots,
                      int64_t n_steps, const double *xs, const double *ys, const int64_t *off, void *dens,
                      void *work_pos0, void *work_neg0, void *work_pos1, void *work_neg1, void *lam_pos0,
-                     void *lam_neg0, void *lam_pos1, void *lam_neg1, double *grad, void *ws, void *adj_ws,
-                     cudaStream_t st) {
+                     void *lam_neg0, void *lam_pos1, void *lam_neg1, double *grad, void *ws, int64_t ws_bytes,
+                     void *adj_ws, cudaStream_t st) {
     DeviceExecutor x;
     x.g = g;
     x.st = st;
@@ -345,6 +346,7 @@ int revolve_backward(const pic_grid *g, void *slots_pos, void *slots_neg, int64_
     x.off = off;
     x.dens = dens;
     x.ws = ws;
+    x.ws_bytes = ws_bytes;
     x.lam[0][0] = lam_pos0;
     x.lam[0][1] = lam_neg0;
     x.lam[1][0] = lam_pos1;

@@ -20,6 +20,8 @@ from .constants import recombination_alpha
 
 _DTYPES = {"float32": N.PIC_F32, "float64": N.PIC_F64}
 _VARIANTS = {"auto": N.PIC_VARIANT_AUTO, "flat": N.PIC_VARIANT_FLAT, "stream": N.PIC_VARIANT_STREAM}
+_DEPOSIT_VARIANTS = {"auto": N.PIC_DEPOSIT_AUTO, "tracks": N.PIC_DEPOSIT_TRACKS, "binned": N.PIC_DEPOSIT_BINNED}
+_EXTRA_FIELDS = ("adjoint_variant", "deposit_variant")
 SHAPE_FIELDS = ("variant", "tile_rows", "planes_per_item", "stages", "consumer_warps", "ctas_per_sm", "steps_per_launch")
 
 
@@ -38,15 +40,18 @@ def nvtx_range(name: str):
 
 
 def apply_shape(g: N.PicGrid, shape: dict | None) -> N.PicGrid:
-    """Sets launch-shape fields of a descriptor from a dict (``variant`` may
-    be ``"auto"``, ``"flat"`` or ``"stream"``); unknown keys raise."""
+    """Sets launch-shape fields of a descriptor from a dict (``variant`` and
+    ``adjoint_variant`` may be ``"auto"``, ``"flat"`` or ``"stream"``,
+    ``deposit_variant`` ``"auto"``, ``"tracks"`` or ``"binned"``); unknown
+    keys raise."""
     for key, val in (shape or {}).items():
-        if key not in SHAPE_FIELDS + ("adjoint_variant",):
-            raise ValueError(f"unknown launch-shape field {key!r}; expected one of {SHAPE_FIELDS + ('adjoint_variant',)}")
-        if key in ("variant", "adjoint_variant") and isinstance(val, str):
-            if val not in _VARIANTS:
-                raise ValueError(f"variant must be one of {sorted(_VARIANTS)}, got {val!r}")
-            val = _VARIANTS[val]
+        if key not in SHAPE_FIELDS + _EXTRA_FIELDS:
+            raise ValueError(f"unknown launch-shape field {key!r}; expected one of {SHAPE_FIELDS + _EXTRA_FIELDS}")
+        names = _DEPOSIT_VARIANTS if key == "deposit_variant" else _VARIANTS
+        if key in ("variant",) + _EXTRA_FIELDS and isinstance(val, str):
+            if val not in names:
+                raise ValueError(f"{key} must be one of {sorted(names)}, got {val!r}")
+            val = names[val]
         setattr(g, key, int(val))
     return g
 

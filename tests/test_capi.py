@@ -57,14 +57,40 @@ def test_binding_covers_the_header(lib):
 
 
 def test_host_only_calls_without_a_gpu(lib):
-    assert lib.pic_abi_version() == 5
+    assert lib.pic_abi_version() == 6
     native = __import__("importlib").import_module(pkg().__name__ + "._native")
-    assert native.ABI_VERSION == 5
-    assert ctypes.sizeof(native.PicGrid) == 192  # 5 int64, 14 double, 9 int32, padded to 8
+    assert native.ABI_VERSION == 6
+    assert ctypes.sizeof(native.PicGrid) == 200  # 5 int64, 14 double, 11 int32, padded to 8
     assert lib.pic_kpitch(406) == 408
     assert lib.pic_kpitch(408) == 408
     assert lib.pic_kpitch(3) == 8
     assert lib.pic_dens_pitch(1068) == 1068 and lib.pic_dens_pitch(25) == 28
+
+
+def test_step_workspace_holds_the_track_lists_of_the_binned_deposition(lib):
+    """The fixed part (tally partials of 152 x 32 blocks, counter, status)
+    plus, for no_xy <= 4096 and truncation boxes of at most 64 cells, a count
+    per 62 x 62-cell tile (padded to 256 bytes), 4096 track indices per tile,
+    and the boxes (4 int16) and factors (2 x 64 of the field type) of 16384
+    tracks."""
+    import importlib
+
+    P = pkg()
+    E = importlib.import_module(P.__name__ + ".engine")
+    beam = dict(E_MeV_u=56.2, voltage_V=300.0, electrode_gap_cm=0.2, pulse_duration_s=540e-6,
+                repetition_rate_hz=50.0, dose_rate_Gy_s=8.91)
+    fixed = 152 * 32 * 4 * 8 + 256
+    for um, r, n in ((10.0, 0.008, 24), (5.0, 0.265, 1068)):
+        cfg = P.SimulationConfig(**dict(beam, grid_size_um=um, sampled_radius_cm=r, seed=1, max_voxels=2e9))
+        assert int(cfg.no_xy) == n
+        g = E.make_grid(cfg)
+        b = ctypes.c_int64()
+        assert lib.pic_step_workspace_bytes(ctypes.byref(g), ctypes.byref(b)) == 0
+        tiles = ((n + 61) // 62) ** 2
+        assert b.value == fixed + (4 * tiles + 255) // 256 * 256 + tiles * 4096 * 4 + 16384 * 8 + 16384 * 128 * 4
+    assert E.apply_shape(g, {"deposit_variant": "binned"}).deposit_variant == 2
+    with pytest.raises(ValueError):
+        E.apply_shape(g, {"deposit_variant": "tiles"})
 
 
 def test_invalid_grid_is_refused_before_any_device_work(lib):
@@ -94,6 +120,10 @@ def test_invalid_grid_is_refused_before_any_device_work(lib):
     assert lib.pic_step_workspace_bytes(ctypes.byref(g), ctypes.byref(b)) == native.PIC_E_INVALID
     assert b"steps_per_launch" in lib.pic_last_error()
     g.steps_per_launch = 256
+    g.deposit_variant = 3
+    assert lib.pic_step_workspace_bytes(ctypes.byref(g), ctypes.byref(b)) == native.PIC_E_INVALID
+    assert b"deposit_variant" in lib.pic_last_error()
+    g.deposit_variant = native.PIC_DEPOSIT_BINNED
     assert lib.pic_step_workspace_bytes(ctypes.byref(g), ctypes.byref(b)) == native.PIC_OK
     assert b.value > 0
     rc = lib.pic_step(ctypes.byref(g), None, None, None, None, None, None, None, None, 0, None)
