@@ -510,12 +510,15 @@ def run_gb300(args):
         dist.barrier()
     t_start = torch.cuda.Event(enable_timing=True)
     t_end = torch.cuda.Event(enable_timing=True)
+    lib = native.load()
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
+        launches0 = lib.pic_kernel_launches()
         t_start.record(stream)
         eng.run_segment(off[args.warmup:] - off[args.warmup], track_base=int(off[args.warmup]))
         t_end.record(stream)
         torch.cuda.synchronize()
+        launches = lib.pic_kernel_launches() - launches0  # the library's own count of its kernel launches
     ms = t_start.elapsed_time(t_end)
     vox = _interior(cfg)
     # all ranks' voxel-steps over the slowest rank's time
@@ -523,14 +526,12 @@ def run_gb300(args):
     ms = replicas.max_over_ranks(ms)
     if world > 1:
         dist.barrier()
-    launches = 2 * int((counts[args.warmup:] > 0).sum()) + int((counts[args.warmup:] == 0).sum())
 
     # dominant kernel: the fused step, one launch per step, event-timed on
     # its own stream, with this step's deposition density applied
     import ctypes
 
     g = eng.grid
-    lib = native.load()
     reps = max(5, min(50, args.steps))
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
     cur = eng.parity

@@ -87,12 +87,18 @@ typedef struct pic_grid {
  * track in the 62 x 62-cell tiles its box meets, then one block per tile sums
  * its tracks' separable Gaussians as outer products in ascending track order
  * and stores each cell once (no atomics on the pairs; two runs give identical
- * pairs). It needs the track lists of the step workspace, so only the calls
+ * pairs). pic_run_segment deposits up to 8 of its steps (65536 tracks) per
+ * pair of launches, into pair buffers in the workspace; its dens0/dens1 then
+ * end as the per-step forms leave them (the last step's pairs if it
+ * deposited, the other buffer zero). It needs the track lists of the step workspace, so only the calls
  * that take one use it (pic_run_segment, the graph capture, the gradient
  * drivers), for no_xy <= 4096 and cutoff_voxels < 31.5 (truncation boxes of
  * at most 64 cells); elsewhere BINNED is refused. AUTO: BINNED
- * where it can run and the grid has at least two tiles per SM (no_xy >= 1055
- * on 152 SMs); otherwise TRACKS, or on small grids
+ * where it can run: for the steps of a segment (pic_run_segment,
+ * pic_adjoint_forward) unless a few tiles would each gather more than ~1024
+ * of a step's tracks; for one step alone (the checkpointed gradient) where
+ * the grid has at least two tiles per SM (no_xy >= 1055 on 152 SMs);
+ * otherwise TRACKS, or on small grids
  * whose steps bring many tracks a scan-tile form (every block scans the
  * step's tracks; one vector atomic per cell and block). */
 #define PIC_DEPOSIT_AUTO 0
@@ -129,9 +135,9 @@ int pic_device_info(int32_t *sm_count, int64_t *total_bytes, int32_t *cc_major, 
 
 /* Bytes of device scratch the fused step needs for this grid (per-block
  * tally partials, a completion counter, a status word and, where the
- * binned deposition can run, its per-tile track lists and the boxes and
- * Gaussian factors of up to 16384 tracks: about 14 MB for a 1068 x 1068
- * float32 grid). The caller allocates it once, zero-filled, and passes it
+ * binned deposition can run, for each of 8 steps its per-tile track lists
+ * and deposition pairs, and the boxes and Gaussian factors of up to 65536
+ * tracks: about 150 MB for a 1068 x 1068 float32 grid). The caller allocates it once, zero-filled, and passes it
  * to pic_step / pic_run_segment; every call leaves its counters at zero again.
  * A workspace of the fixed part alone (ABI 5's size) is still accepted: the
  * deposition then runs without the binned form. */
@@ -425,6 +431,13 @@ int pic_graph_create(const pic_grid *g, void *pos0, void *neg0, void *pos1, void
                      void *workspace, int64_t workspace_bytes, uintptr_t stream, uintptr_t *graph_out);
 int pic_graph_launch(uintptr_t graph, uintptr_t stream);
 int pic_graph_destroy(uintptr_t graph);
+
+/* Kernel launches this library has issued in this process: every launch of
+ * every entry point, and for each replay of a graph (pic_graph_launch) the
+ * launches captured into it (those do not count when captured). Host-only;
+ * no counterpart in the reference: the figure a benchmark reports as its
+ * kernel count. */
+int64_t pic_kernel_launches(void);
 
 /*
  * Batched runs: many independent grids advanced together.

@@ -27,7 +27,7 @@ PIC_DEPOSIT_AUTO = 0
 PIC_DEPOSIT_TRACKS = 1
 PIC_DEPOSIT_BINNED = 2
 # pic_abi_version() of the library these structures mirror
-ABI_VERSION = 6
+ABI_VERSION = 7
 
 _LIB_PATH = Path(__file__).resolve().parent / "_build" / "libpic_gb300.so"
 _lock = threading.Lock()
@@ -201,6 +201,7 @@ EXPORTS = {
     ),
     "pic_graph_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "pic_graph_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "pic_kernel_launches": (ctypes.c_int64, []),
 }
 
 

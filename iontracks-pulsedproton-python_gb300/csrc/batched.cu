@@ -390,6 +390,7 @@ static int launch_persistent(const BatchLaunch &L, const int64_t *sto, const int
     void *args[] = {&p};
     e = cudaLaunchCooperativeKernel((const void *)batched_persistent_kernel<T, I>, dim3(grid), dim3(256), args, 0, st);
     if (e != cudaSuccess) return set_cuda_error("cudaLaunchCooperativeKernel(batched_persistent_kernel)", e);
+    count_launches(1);
     return PIC_OK;
 }
 

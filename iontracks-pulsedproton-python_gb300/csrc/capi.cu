@@ -5,9 +5,11 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <atomic>
 #include <cmath>
 #include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "pic_internal.h"
@@ -25,9 +27,31 @@ int set_cuda_error(const char *what, cudaError_t e) {
     return set_error(PIC_E_CUDA, std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
 }
 
+// Kernel launches this library has issued. A thread capturing a graph
+// (pic_graph_create, pic_capture_begin .. _end) counts its launches into the
+// graph instead, and every replay of the graph adds them.
+static std::atomic<int64_t> g_launches{0};
+static thread_local int64_t t_captured = -1;  // >= 0 while this thread captures
+static std::mutex g_graph_mu;
+static std::unordered_map<uintptr_t, int64_t> g_graph_launches;
+
+void count_launches(int64_t n) {
+    if (t_captured >= 0)
+        t_captured += n;
+    else
+        g_launches += n;
+}
+
+static void graph_launches_set(uintptr_t exec, int64_t n) {
+    std::lock_guard<std::mutex> lock(g_graph_mu);
+    g_graph_launches[exec] = n;
+}
+
 int check_launch(const char *what) {
     cudaError_t e = cudaGetLastError();
-    return e == cudaSuccess ? PIC_OK : set_cuda_error(what, e);
+    if (e != cudaSuccess) return set_cuda_error(what, e);
+    count_launches(1);
+    return PIC_OK;
 }
 
 int64_t step_grid_cap(int f64) {
@@ -202,6 +226,39 @@ static int run_loop(const pic_grid *g, void *pos0, void *neg0, void *pos1, void 
         }
         return PIC_OK;
     }
+    int64_t most = 0;
+    for (int64_t s = 0; s < n_steps; ++s) most = std::max(most, off[s + 1] - off[s]);
+    if (most > 0 && most <= kBinTracks && deposit_binned(g, ws, ws_bytes, most)) {
+        // the binned deposition of up to kBinSteps steps (kBinTracks tracks)
+        // at a time into the workspace's pair buffers, then those steps
+        const void *dp[kBinSpan];
+        const void *last_pairs = nullptr;  // the pairs of the segment's last step (null: no tracks)
+        for (int64_t s0 = 0; s0 < n_steps;) {
+            int64_t nd = 0;
+            const int64_t s1 = next_deposit_group(off, s0, n_steps, &nd);
+            int rc = launch_deposit_steps(g, xs, ys, off, s0, s1, counts, ws, nullptr, dp, st);
+            if (rc) return rc;
+            for (int64_t s = s0; s < s1; ++s) {
+                const int bi = (int)((parity + s) & 1);
+                if ((rc = launch_step(g, pos[bi], neg[bi], pos[bi ^ 1], neg[bi ^ 1], dp[s - s0], nullptr, tally + 4 * s,
+                                      ws, st)))
+                    return rc;
+            }
+            if (s1 == n_steps) last_pairs = dp[s1 - 1 - s0];
+            s0 = s1;
+        }
+        // The caller's pair buffers, as the per-step forms leave them: the
+        // last step's pairs if it deposited, and a zero buffer for the step
+        // after the segment.
+        const int64_t pb = dens_pitch(g->no_xy) * 2 * g->no_xy * (g->dtype == PIC_F64 ? 8 : 4);
+        const int last = (int)((dens_parity + n_steps - 1) & 1);
+        if (last_pairs) {
+            cudaError_t e = cudaMemcpyAsync(dens[last], last_pairs, (size_t)pb, cudaMemcpyDeviceToDevice, st);
+            if (e != cudaSuccess) return set_cuda_error("cudaMemcpyAsync(deposition pairs)", e);
+        }
+        cudaError_t e = cudaMemsetAsync(dens[last ^ 1], 0, (size_t)pb, st);
+        return e == cudaSuccess ? PIC_OK : set_cuda_error("cudaMemsetAsync(deposition pairs)", e);
+    }
     for (int64_t s = 0; s < n_steps; ++s) {
         const int bi = (int)((parity + s) & 1), bo = bi ^ 1;
         const int di = (int)((dens_parity + s) & 1);
@@ -282,7 +339,7 @@ const char *pic_last_error(void) { return g_last_error.c_str(); }
 // double, 9 int32, padded to 8 bytes).
 static_assert(sizeof(pic_grid) == 200, "pic_grid layout changed: bump pic_abi_version and the bindings");
 
-int pic_abi_version(void) { return 6; }
+int pic_abi_version(void) { return 7; }
 
 int64_t pic_kpitch(int64_t nzb) { return (nzb + 7) / 8 * 8; }
 
@@ -476,6 +533,43 @@ int pic_adjoint_forward(const pic_grid *g, void *pos0, void *neg0, void *pos1, v
     }
     void *pos[2] = {pos0, pos1}, *neg[2] = {neg0, neg1};
     char *D = static_cast<char *>(dens_keep);
+    auto checkpoint = [&](int64_t s) -> int {
+        if (s % ckpt_every != 0) return PIC_OK;
+        const int b = (int)(s & 1);
+        const int64_t c = s / ckpt_every;
+        cudaError_t e = cudaMemcpyAsync(static_cast<char *>(ckpt_pos) + c * state_stride * es, pos[b],
+                                        (size_t)(field * es), cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(static_cast<char *>(ckpt_neg) + c * state_stride * es, neg[b], (size_t)(field * es),
+                                cudaMemcpyDeviceToDevice, st);
+        return e == cudaSuccess ? PIC_OK : set_cuda_error("cudaMemcpyAsync(checkpoint)", e);
+    };
+    int64_t most = 0;
+    for (int64_t s = 0; s < n_steps; ++s) most = std::max(most, track_offsets[s + 1] - track_offsets[s]);
+    if (most > 0 && most <= kBinTracks && deposit_binned(g, workspace, workspace_bytes, most)) {
+        // each launch pair deposits up to kBinSteps steps straight into their
+        // kept slots
+        const void *dp[kBinSpan];
+        void *targets[kBinSteps];
+        int64_t d = 0;
+        for (int64_t s0 = 0; s0 < n_steps;) {
+            int64_t nd = 0;
+            const int64_t s1 = next_deposit_group(track_offsets, s0, n_steps, &nd);
+            for (int64_t k = 0; k < nd; ++k) targets[k] = D + (d + k) * dslot * es;
+            if ((rc = launch_deposit_steps(g, xs, ys, track_offsets, s0, s1, counts, workspace, targets, dp, st)))
+                return rc;
+            d += nd;
+            for (int64_t s = s0; s < s1; ++s) {
+                const int b = (int)(s & 1);
+                if ((rc = checkpoint(s))) return rc;
+                if ((rc = launch_step(g, pos[b], neg[b], pos[b ^ 1], neg[b ^ 1], dp[s - s0], nullptr, tally + 4 * s,
+                                      workspace, st)))
+                    return rc;
+            }
+            s0 = s1;
+        }
+        return PIC_OK;
+    }
     int64_t d = 0;
     for (int64_t s = 0; s < n_steps; ++s) {
         const int b = (int)(s & 1);
@@ -683,8 +777,11 @@ int pic_graph_create(const pic_grid *g, void *pos0, void *neg0, void *pos1, void
         if (own) cudaStreamDestroy(own);
         return set_cuda_error("cudaStreamBeginCapture", e);
     }
+    t_captured = 0;
     rc = run_loop(g, pos0, neg0, pos1, neg1, parity, n_steps, xs, ys, track_offsets, dens0, dens1, dens_parity,
                   counts, tally, workspace, workspace_bytes, st);
+    const int64_t captured = t_captured;
+    t_captured = -1;
     e = cudaStreamEndCapture(st, &graph);
     if (own) cudaStreamDestroy(own);
     if (rc) {
@@ -697,6 +794,7 @@ int pic_graph_create(const pic_grid *g, void *pos0, void *neg0, void *pos1, void
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return set_cuda_error("cudaGraphInstantiate", e);
     *graph_out = reinterpret_cast<uintptr_t>(exec);
+    graph_launches_set(*graph_out, captured);
     return PIC_OK;
 }
 
@@ -706,7 +804,9 @@ int pic_capture_begin(uintptr_t stream) {
     if (st == nullptr || st == cudaStreamLegacy || st == cudaStreamPerThread)
         return set_error(PIC_E_INVALID, "capture needs a stream created by the caller (not the default stream)");
     cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
-    return e == cudaSuccess ? PIC_OK : set_cuda_error("cudaStreamBeginCapture", e);
+    if (e != cudaSuccess) return set_cuda_error("cudaStreamBeginCapture", e);
+    t_captured = 0;
+    return PIC_OK;
 }
 
 int pic_capture_end(uintptr_t stream, uintptr_t *graph_out) {
@@ -714,6 +814,8 @@ int pic_capture_end(uintptr_t stream, uintptr_t *graph_out) {
     if (!graph_out) return set_error(PIC_E_INVALID, "graph_out is null");
     *graph_out = 0;
     cudaGraph_t graph = nullptr;
+    const int64_t captured = t_captured < 0 ? 0 : t_captured;
+    t_captured = -1;
     cudaError_t e = cudaStreamEndCapture(reinterpret_cast<cudaStream_t>(stream), &graph);
     if (e != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);
@@ -724,6 +826,7 @@ int pic_capture_end(uintptr_t stream, uintptr_t *graph_out) {
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return set_cuda_error("cudaGraphInstantiate", e);
     *graph_out = reinterpret_cast<uintptr_t>(exec);
+    graph_launches_set(*graph_out, captured);
     return PIC_OK;
 }
 
@@ -824,11 +927,25 @@ int pic_graph_launch(uintptr_t graph, uintptr_t stream) {
     NvtxRange nvtx_range("pic_graph_launch");
     if (!graph) return set_error(PIC_E_INVALID, "graph handle is null");
     cudaError_t e = cudaGraphLaunch(reinterpret_cast<cudaGraphExec_t>(graph), reinterpret_cast<cudaStream_t>(stream));
-    return e == cudaSuccess ? PIC_OK : set_cuda_error("cudaGraphLaunch", e);
+    if (e != cudaSuccess) return set_cuda_error("cudaGraphLaunch", e);
+    int64_t n = 0;
+    {
+        std::lock_guard<std::mutex> lock(g_graph_mu);
+        auto it = g_graph_launches.find(graph);
+        if (it != g_graph_launches.end()) n = it->second;
+    }
+    count_launches(n);
+    return PIC_OK;
 }
+
+int64_t pic_kernel_launches(void) { return g_launches.load(); }
 
 int pic_graph_destroy(uintptr_t graph) {
     if (!graph) return PIC_OK;
+    {
+        std::lock_guard<std::mutex> lock(g_graph_mu);
+        g_graph_launches.erase(graph);
+    }
     cudaError_t e = cudaGraphExecDestroy(reinterpret_cast<cudaGraphExec_t>(graph));
     return e == cudaSuccess ? PIC_OK : set_cuda_error("cudaGraphExecDestroy", e);
 }

@@ -83,8 +83,10 @@ __global__ void __launch_bounds__(kDepThreads) deposit_tile_kernel(const double 
 // binning's atomics ran in: two runs give identical pairs. Every cell of a
 // tile some track reaches is stored once, without atomics; a tile no track
 // reaches is left as it is (zero: the buffer is zero on entry, as for the
-// other forms). A step with more than kBinGroup tracks runs in groups, the
-// later ones adding to the cells the first stored.
+// other forms). One pair of launches serves up to kBinSteps steps of a
+// segment, one slot each (BinLaunch), which gives the GPU eight times the
+// blocks of one step; a step with more than kBinTracks tracks runs in pieces,
+// the later ones adding to the cells the first stored.
 constexpr int kBinC = kBinOut + 2;  // density tile side: output cells and a one-cell halo
 constexpr int kBinThreads = 256;    // 16 x 16 threads, 4 x 4 density cells each
 constexpr int kBinBatch = 16;       // tracks whose factors are staged together
@@ -92,19 +94,37 @@ static_assert(kBinC == 64 && kBinBox == 64, "a thread's 4 x 4 cells of 16 x 16 t
 
 template <typename T>
 struct DepBins {
-    int *count;    // [tiles]
-    int *list;     // [tiles][kBinCap], track indices within the group
-    short4 *box;   // [kBinGroup]: lo_i, hi_i, lo_j, hi_j (the truncation box)
-    T *fac;        // [kBinGroup][2][kBinBox]: gx from lo_i, G gy from lo_j
-    int64_t tps;   // tiles per side
+    int *count;     // [kBinSteps][tiles]
+    int *list;      // [kBinSteps][tiles][kBinCap], track indices within the launch
+    short4 *box;    // [kBinTracks]: lo_i, hi_i, lo_j, hi_j (the truncation box)
+    T *fac;         // [kBinTracks][2][kBinBox]: gx from lo_i, G gy from lo_j
+    char *dens;     // [kBinSteps] pair buffers of bin_dens_bytes
+    int64_t tps;    // tiles per side
+    int64_t tiles;  // tps^2
 };
 template <typename T>
 inline DepBins<T> dep_bins(void *ws, int64_t n) {
+    const int64_t es = sizeof(T);
     char *b = static_cast<char *>(ws) + kWorkspaceBytes;
     char *list = b + bin_count_bytes(n), *box = list + bin_list_bytes(n), *fac = box + bin_box_bytes();
+    char *dens = fac + bin_fac_bytes(es);
+    const int64_t t = bin_tiles_per_side(n);
     return DepBins<T>{reinterpret_cast<int *>(b), reinterpret_cast<int *>(list), reinterpret_cast<short4 *>(box),
-                      reinterpret_cast<T *>(fac), bin_tiles_per_side(n)};
+                      reinterpret_cast<T *>(fac), dens, t, t * t};
 }
+
+// The slots of one pair of binned launches: slot k holds the launch's tracks
+// [first[k], first[k + 1]) (counted from the launch's first track) and writes
+// its pairs to dens[k]. add = 0: every cell of every tile is stored (zero
+// where no track reaches); add = 1 (a later piece of one step): the sums are
+// added to the cells and tiles no track reaches are left alone.
+template <typename T>
+struct BinLaunch {
+    int64_t first[kBinSteps + 1];
+    pair_t<T> *dens[kBinSteps];
+    int slots;
+    int add;
+};
 
 // The truncation box [lo, hi) of a track along one axis, clipped to the grid
 // (solver_numba.py:86-89).
@@ -124,10 +144,11 @@ __device__ __forceinline__ void track_box(double c, double cut, int64_t n, int64
 constexpr int kBinWarpTracks = 4;
 template <typename T>
 __global__ void __launch_bounds__(256) deposit_bin_kernel(const double *__restrict__ xs,
-                                                          const double *__restrict__ ys, int64_t m, int64_t n,
-                                                          double cut, T h2b2, T gfac, uint32_t *__restrict__ counts,
-                                                          DepBins<T> bins) {
+                                                          const double *__restrict__ ys, int64_t n, double cut,
+                                                          T h2b2, T gfac, uint32_t *__restrict__ counts,
+                                                          DepBins<T> bins, BinLaunch<T> L) {
     const int lane = threadIdx.x & 31, ax = lane & 1;
+    const int64_t m = L.first[L.slots];
     const int64_t t0 = ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * kBinWarpTracks;
     if (t0 >= m) return;
     const int64_t tl = t0 + (lane >> 1);
@@ -184,19 +205,23 @@ __global__ void __launch_bounds__(256) deposit_bin_kernel(const double *__restri
     const int tj1 = hi_j / kBinOut < T_ - 1 ? hi_j / kBinOut : T_ - 1;
     const int nj = tj1 - tj0 + 1, ntiles = (ti1 - ti0 + 1) * nj;
     const int t = (int)(t0 + q);
+    int k = 0;  // the track's slot
+    while (k + 1 < L.slots && L.first[k + 1] <= t) ++k;
+    int *count = bins.count + k * bins.tiles;
+    int *list = bins.list + k * bins.tiles * kBinCap;
     // the first two tiles of this lane: both counters bumped before either
-    // slot is used (one round trip), the rest one at a time
+    // list entry is written (one round trip), the rest one at a time
     const int qa = ax, qb = ax + 2;
     const int64_t ta = qa < ntiles ? (int64_t)(ti0 + qa / nj) * T_ + tj0 + qa % nj : -1;
     const int64_t tb = qb < ntiles ? (int64_t)(ti0 + qb / nj) * T_ + tj0 + qb % nj : -1;
-    const int sa = ta >= 0 ? atomicAdd(bins.count + ta, 1) : kBinCap;
-    const int sb = tb >= 0 ? atomicAdd(bins.count + tb, 1) : kBinCap;
-    if (sa < kBinCap) bins.list[ta * kBinCap + sa] = t;
-    if (sb < kBinCap) bins.list[tb * kBinCap + sb] = t;
+    const int sa = ta >= 0 ? atomicAdd(count + ta, 1) : kBinCap;
+    const int sb = tb >= 0 ? atomicAdd(count + tb, 1) : kBinCap;
+    if (sa < kBinCap) list[ta * kBinCap + sa] = t;
+    if (sb < kBinCap) list[tb * kBinCap + sb] = t;
     for (int qq = ax + 4; qq < ntiles; qq += 2) {
         const int64_t tile = (int64_t)(ti0 + qq / nj) * T_ + tj0 + qq % nj;
-        const int slot = atomicAdd(bins.count + tile, 1);
-        if (slot < kBinCap) bins.list[tile * kBinCap + slot] = t;
+        const int e = atomicAdd(count + tile, 1);
+        if (e < kBinCap) list[tile * kBinCap + e] = t;
     }
 }
 
@@ -262,9 +287,8 @@ struct BinSmem {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(kBinThreads) deposit_binned_kernel(int64_t m, int64_t n, int64_t dp,
-                                                                     pair_t<T> *__restrict__ dens, DepBins<T> bins,
-                                                                     int add) {
+__global__ void __launch_bounds__(kBinThreads) deposit_binned_kernel(int64_t n, int64_t dp, DepBins<T> bins,
+                                                                     BinLaunch<T> L) {
     extern __shared__ __align__(16) unsigned char bin_smem[];
     using S = BinSmem<T>;
     constexpr int C = kBinChunk, FB = kBinBatch * 2 * kBinC;  // factors per buffer
@@ -276,12 +300,25 @@ __global__ void __launch_bounds__(kBinThreads) deposit_binned_kernel(int64_t m, 
     __shared__ int s_count;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int64_t tile = blockIdx.x;
+    const int slot = (int)(blockIdx.x / bins.tiles);
+    const int64_t tile = blockIdx.x - slot * bins.tiles;
     const int i0 = (int)((tile / bins.tps) * kBinOut - 1), j0 = (int)((tile % bins.tps) * kBinOut - 1);
-    if (tid == 0) s_count = bins.count[tile];
+    int *count = bins.count + slot * bins.tiles + tile;
+    const int *tile_list = bins.list + (slot * bins.tiles + tile) * kBinCap;
+    pair_t<T> *__restrict__ dens = L.dens[slot];
+    const int add = L.add;
+    if (tid == 0) s_count = *count;
     __syncthreads();
     const int cnt = s_count;
-    if (cnt == 0) return;  // no track reaches the tile: its cells stay as they are
+    if (cnt == 0) {
+        // no track reaches the tile: zero pairs (or, adding, nothing)
+        if (!add)
+            for (int q = tid; q < kBinOut * kBinOut; q += kBinThreads) {
+                const int64_t i = i0 + 1 + q / kBinOut, j = j0 + 1 + q % kBinOut;
+                if (i < n && j < n) dens[i * dp + j] = pair_t<T>{T(0), T(0)};
+            }
+        return;
+    }
 
     const int ty = tid >> 4, tx = tid & 15;  // density cells (4 ty + a, 4 tx + b)
     BinAcc<T> acc;
@@ -342,8 +379,7 @@ __global__ void __launch_bounds__(kBinThreads) deposit_binned_kernel(int64_t m, 
     };
 
     if (cnt <= kBinCap) {
-        const int *src = bins.list + tile * kBinCap;
-        for (int q = tid; q < cnt; q += kBinThreads) list[q] = src[q];
+        for (int q = tid; q < cnt; q += kBinThreads) list[q] = tile_list[q];
         __syncthreads();
         // ascending track order: rank sort for short lists, bitonic otherwise
         if (cnt <= kBinThreads) {
@@ -377,12 +413,13 @@ __global__ void __launch_bounds__(kBinThreads) deposit_binned_kernel(int64_t m, 
         __syncthreads();
         for (int c0 = 0; c0 < cnt; c0 += C) sum_chunk(list + c0, cnt - c0 < C ? cnt - c0 : C);
     } else {
-        // more tracks than the list holds: scan every track in order, a
+        // more tracks than the list holds: scan the slot's tracks in order, a
         // chunk of kBinThreads at a time, keeping those whose box meets the tile
-        for (int64_t c0 = 0; c0 < m; c0 += kBinThreads) {
+        const int64_t m0 = L.first[slot], m1 = L.first[slot + 1];
+        for (int64_t c0 = m0; c0 < m1; c0 += kBinThreads) {
             const int64_t t = c0 + tid;
             bool hit = false;
-            if (t < m) {
+            if (t < m1) {
                 const short4 b = bins.box[t];
                 hit = b.x < b.y && b.z < b.w && b.x < i0 + kBinC && b.y > i0 && b.z < j0 + kBinC && b.w > j0;
             }
@@ -431,13 +468,12 @@ __global__ void __launch_bounds__(kBinThreads) deposit_binned_kernel(int64_t m, 
             *d = v;
         }
     }
-    if (tid == 0) bins.count[tile] = 0;  // the next binning starts from zero
+    if (tid == 0) *count = 0;  // the next binning starts from zero
 }
 
 template <typename T>
-int launch_binned(const pic_grid *g, const double *xs, const double *ys, int64_t m, void *dens, uint32_t *counts,
-                  void *ws, cudaStream_t st) {
-    const DepBins<T> bins = dep_bins<T>(ws, g->no_xy);
+int binned_launches(const pic_grid *g, const double *xs, const double *ys, uint32_t *counts, const DepBins<T> &bins,
+                    const BinLaunch<T> &L, cudaStream_t st) {
     constexpr int smem = BinSmem<T>::kBytes;
     static int configured = 0;  // per instantiation
     if (smem > 48 * 1024 && !configured) {
@@ -446,19 +482,88 @@ int launch_binned(const pic_grid *g, const double *xs, const double *ys, int64_t
         if (e != cudaSuccess) return set_cuda_error("cudaFuncSetAttribute(deposit_binned_kernel)", e);
         configured = 1;
     }
-    for (int64_t g0 = 0; g0 < m; g0 += kBinGroup) {
-        const int64_t mg = m - g0 < kBinGroup ? m - g0 : kBinGroup;
-        const int64_t warps = (mg + kBinWarpTracks - 1) / kBinWarpTracks;
-        deposit_bin_kernel<T><<<(unsigned)((warps + 7) / 8), 256, 0, st>>>(xs + g0, ys + g0, mg, g->no_xy,
-                                                                        g->cutoff_voxels, (T)g->h2_over_b2,
-                                                                        (T)g->gaussian_factor, counts, bins);
-        int rc = check_launch("deposit_bin_kernel");
+    const int64_t warps = (L.first[L.slots] + kBinWarpTracks - 1) / kBinWarpTracks;
+    deposit_bin_kernel<T><<<(unsigned)((warps + 7) / 8), 256, 0, st>>>(
+        xs, ys, g->no_xy, g->cutoff_voxels, (T)g->h2_over_b2, (T)g->gaussian_factor, counts, bins, L);
+    int rc = check_launch("deposit_bin_kernel");
+    if (rc) return rc;
+    deposit_binned_kernel<T><<<(unsigned)(L.slots * bins.tiles), kBinThreads, smem, st>>>(
+        g->no_xy, dens_pitch(g->no_xy), bins, L);
+    return check_launch("deposit_binned_kernel");
+}
+
+// One step's tracks into the caller's pairs, in pieces of kBinTracks.
+template <typename T>
+int launch_binned(const pic_grid *g, const double *xs, const double *ys, int64_t m, void *dens, uint32_t *counts,
+                  void *ws, cudaStream_t st) {
+    const DepBins<T> bins = dep_bins<T>(ws, g->no_xy);
+    for (int64_t g0 = 0; g0 < m; g0 += kBinTracks) {
+        BinLaunch<T> L{};
+        L.slots = 1;
+        L.first[0] = 0;
+        L.first[1] = m - g0 < kBinTracks ? m - g0 : kBinTracks;
+        L.dens[0] = static_cast<pair_t<T> *>(dens);
+        L.add = g0 > 0;
+        int rc = binned_launches<T>(g, xs + g0, ys + g0, counts, bins, L, st);
         if (rc) return rc;
-        deposit_binned_kernel<T><<<(unsigned)(bins.tps * bins.tps), kBinThreads, smem, st>>>(
-            mg, g->no_xy, dens_pitch(g->no_xy), (pair_t<T> *)dens, bins, g0 > 0);
-        if ((rc = check_launch("deposit_binned_kernel"))) return rc;
     }
     return PIC_OK;
+}
+
+template <typename T>
+int launch_binned_steps(const pic_grid *g, const double *xs, const double *ys, const int64_t *off, int64_t s0,
+                        int64_t s1, uint32_t *counts, void *ws, void *const *targets, const void **dens,
+                        cudaStream_t st) {
+    const DepBins<T> bins = dep_bins<T>(ws, g->no_xy);
+    const int64_t slot_bytes = bin_dens_bytes(g->no_xy, sizeof(T));
+    BinLaunch<T> L{};
+    L.add = 0;
+    int k = 0;
+    for (int64_t s = s0; s < s1; ++s) {
+        dens[s - s0] = nullptr;
+        if (off[s + 1] == off[s]) continue;
+        if (k == kBinSteps) return set_error(PIC_E_INVALID, "more than kBinSteps depositing steps in one launch");
+        L.first[k] = off[s] - off[s0];
+        L.dens[k] = reinterpret_cast<pair_t<T> *>(targets ? static_cast<char *>(targets[k]) : bins.dens + k * slot_bytes);
+        dens[s - s0] = L.dens[k];
+        ++k;
+    }
+    if (k == 0) return PIC_OK;
+    L.slots = k;
+    L.first[k] = off[s1] - off[s0];
+    if (L.first[k] > kBinTracks) return set_error(PIC_E_INVALID, "more than kBinTracks tracks in one launch");
+    return binned_launches<T>(g, xs + off[s0], ys + off[s0], counts, bins, L, st);
+}
+
+int launch_deposit_steps(const pic_grid *g, const double *xs, const double *ys, const int64_t *off, int64_t s0,
+                         int64_t s1, uint32_t *counts, void *ws, void *const *targets, const void **dens,
+                         cudaStream_t st) {
+    return g->dtype == PIC_F64 ? launch_binned_steps<double>(g, xs, ys, off, s0, s1, counts, ws, targets, dens, st)
+                               : launch_binned_steps<float>(g, xs, ys, off, s0, s1, counts, ws, targets, dens, st);
+}
+
+int64_t next_deposit_group(const int64_t *off, int64_t s0, int64_t n_steps, int64_t *n_dep) {
+    int64_t s1 = s0, nd = 0;
+    while (s1 < n_steps && s1 - s0 < kBinSpan) {
+        const int64_t m = off[s1 + 1] - off[s1];
+        if (m > 0 && (nd == kBinSteps || off[s1 + 1] - off[s0] > kBinTracks)) break;
+        nd += m > 0;
+        ++s1;
+    }
+    *n_dep = nd;
+    return s1;
+}
+
+bool deposit_binned(const pic_grid *g, const void *ws, int64_t ws_bytes, int64_t most) {
+    const int64_t bin_bytes = dep_bin_bytes(g);
+    const bool bins = ws && bin_bytes > 0 && ws_bytes >= kWorkspaceBytes + bin_bytes;
+    if (!bins || g->deposit_variant == PIC_DEPOSIT_TRACKS) return false;
+    if (g->deposit_variant == PIC_DEPOSIT_BINNED) return true;
+    const int64_t tiles = bin_tiles_per_side(g->no_xy) * bin_tiles_per_side(g->no_xy);
+    if (most < 0) return tiles >= (int64_t)kBinAutoTilesPerSm * sm_count();  // one step alone
+    // grouped: enough blocks for the SMs, or tiles short enough for one block
+    const double per_axis = (2.0 * g->cutoff_voxels + kBinC) / kBinOut;  // tiles a track meets along an axis
+    return tiles * kBinSteps >= sm_count() || (double)most * per_axis * per_axis / (double)tiles <= kBinAutoPerTile;
 }
 
 // Track-tile pairs a step's deposition may scan in the tile form: beyond it
@@ -475,15 +580,11 @@ constexpr int64_t kDepTileMinBlocks = 1024;
 int launch_deposit(const pic_grid *g, const double *xs, const double *ys, int64_t m, void *dens, uint32_t *counts,
                    cudaStream_t st, void *ws, int64_t ws_bytes) {
     if (m <= 0) return PIC_OK;
-    const int64_t bin_bytes = dep_bin_bytes(g);
-    const bool bins = ws && bin_bytes > 0 && ws_bytes >= kWorkspaceBytes + bin_bytes;
-    if (g->deposit_variant == PIC_DEPOSIT_BINNED && !bins)
+    if (g->deposit_variant == PIC_DEPOSIT_BINNED && !deposit_binned(g, ws, ws_bytes, -1))
         return set_error(PIC_E_INVALID,
                          "the binned deposition needs the step workspace of pic_step_workspace_bytes (pic_run_segment "
                          "and the gradient drivers; no_xy <= 4096, cutoff_voxels < 31.5)");
-    const int64_t tps = bin_tiles_per_side(g->no_xy);
-    if (g->deposit_variant == PIC_DEPOSIT_BINNED ||
-        (g->deposit_variant == PIC_DEPOSIT_AUTO && bins && tps * tps >= (int64_t)kBinAutoTilesPerSm * sm_count()))
+    if (deposit_binned(g, ws, ws_bytes, -1))
         return g->dtype == PIC_F64 ? launch_binned<double>(g, xs, ys, m, dens, counts, ws, st)
                                    : launch_binned<float>(g, xs, ys, m, dens, counts, ws, st);
     const int64_t tiles = deposit_tiles(g->no_xy);

@@ -213,6 +213,7 @@ int launch_t(const pic_grid *g, void *const pos[2], void *const neg[2], int pari
     cfg.numAttrs = 1;
     cudaError_t e = cudaLaunchKernelEx(&cfg, multistep_kernel<T, I>, p);
     if (e != cudaSuccess) return set_cuda_error("cudaLaunchKernelEx(multistep_kernel)", e);
+    count_launches(1);
     return PIC_OK;
 }
 

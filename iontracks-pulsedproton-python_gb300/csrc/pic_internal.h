@@ -148,32 +148,47 @@ int launch_deposit(const pic_grid *g, const double *xs, const double *ys, int64_
 // track's Gaussian row and column factors once and lists the track in the
 // tiles of kBinOut x kBinOut cells its written box meets; then one block per
 // tile sums its tracks' outer products in a fixed order and stores each cell
-// once. Its scratch sits in the step workspace behind kWorkspaceBytes: a
-// count per tile (zero between steps; the tile's block clears it), kBinCap
-// track indices per tile (a tile with more scans every track), and the boxes
-// and factors of up to kBinGroup tracks (a step with more runs in groups).
+// once. One pair of launches serves up to kBinSteps steps of a segment (their
+// tracks together at most kBinTracks), each step a slot with its own track
+// lists and its own pair buffer in the workspace. The scratch sits in the
+// step workspace behind kWorkspaceBytes: a count per slot and tile (zero
+// between launches; the tile's block clears it), kBinCap track indices per
+// slot and tile (a tile with more scans its slot's tracks), the boxes and
+// factors of kBinTracks tracks, and kBinSteps pair buffers.
 constexpr int kBinOut = 62;
 constexpr int kBinCap = 4096;
-constexpr int kBinGroup = 16384;
+constexpr int kBinSteps = 8;
+constexpr int kBinTracks = 65536;
 constexpr int kBinBox = 64;               // factors kept per track and axis
 constexpr int64_t kBinMaxNoXy = 4096;     // largest grid with track lists
-// AUTO takes the binned form where a grid's tiles give at least this many
-// blocks per SM (no_xy >= 1055 on 152 SMs): on smaller grids the per-track
-// warps, spread over every SM, finish first (measured on GB300: 1068^2 with
-// 8 500 tracks a step 45 against 64 us; 608^2 with 2 700 even; 608^2 with
-// 27 000 and 208^2 with 300 slower in tiles)
+// AUTO: the binned form for a segment's steps (up to eight per launch pair)
+// where those launches give every SM a block (tiles x 8 >= SMs) or a tile
+// meets about kBinAutoPerTile tracks of a step at most, so one block's serial
+// sum stays short. Measured on GB300, per step against the per-track warps:
+// 1068^2 with 8 500 tracks 20 against 64 us, 608^2 with 27 000 106 against
+// 133, 208^2 with 300 6 against 11, 128^2 with 109 4.5 against 7.7, 48^2
+// with 101 3.5 against 3.8 and with ~290 (~630 a tile) a 10 um column's
+// whole run 18.3 against 22.1 ms; 108^2 with 632 (~350 a tile) 8.1 against
+// 6.9; 48^2 with 1 011 (~2 200 a tile) 16 against 10.5. One step alone (the
+// checkpointed gradient) only where the grid's tiles give at least
+// kBinAutoTilesPerSm blocks per SM (no_xy >= 1055 on 152 SMs; 608^2 with
+// 27 000 tracks 158 against 132 us, 208^2 20 against 11).
 constexpr int kBinAutoTilesPerSm = 2;
+constexpr int kBinAutoPerTile = 1024;
+constexpr int kBinSpan = 256;  // steps one launch pair may span, idle steps between included
 inline int64_t bin_tiles_per_side(int64_t n) { return (n + kBinOut - 1) / kBinOut; }
 inline int64_t bin_align(int64_t b) { return (b + 255) / 256 * 256; }
 inline int64_t bin_count_bytes(int64_t n) {
     const int64_t t = bin_tiles_per_side(n);
-    return bin_align(t * t * 4);
+    return bin_align(kBinSteps * t * t * 4);
 }
 inline int64_t bin_list_bytes(int64_t n) {
     const int64_t t = bin_tiles_per_side(n);
-    return t * t * kBinCap * 4;
+    return kBinSteps * t * t * kBinCap * 4;
 }
-inline int64_t bin_box_bytes() { return bin_align((int64_t)kBinGroup * 8); }
+inline int64_t bin_box_bytes() { return bin_align((int64_t)kBinTracks * 8); }
+inline int64_t bin_fac_bytes(int64_t es) { return (int64_t)kBinTracks * 2 * kBinBox * es; }
+inline int64_t bin_dens_bytes(int64_t n, int64_t es) { return bin_align(n * dens_pitch(n) * 2 * es); }
 // A grid takes the binned form when its track lists fit (no_xy <= 4096) and
 // every truncation box, [ceil(c - cut), floor(c + cut)], spans at most
 // kBinBox cells (floor(2 cut) + 1 of them at most).
@@ -183,9 +198,26 @@ inline bool bin_eligible(const pic_grid *g) {
 inline int64_t dep_bin_bytes(const pic_grid *g) {
     if (!bin_eligible(g)) return 0;
     const int64_t es = g->dtype == PIC_F64 ? 8 : 4;
-    return bin_count_bytes(g->no_xy) + bin_list_bytes(g->no_xy) + bin_box_bytes() + (int64_t)kBinGroup * 2 * kBinBox * es;
+    return bin_count_bytes(g->no_xy) + bin_list_bytes(g->no_xy) + bin_box_bytes() + bin_fac_bytes(es) +
+           kBinSteps * bin_dens_bytes(g->no_xy, es);
 }
-using BatchLaunch = pic_batch_launch;
+// Whether the deposition takes the binned form for this grid and workspace:
+// for a segment's steps together (most = the most tracks one of them has),
+// or with most < 0 for one step alone.
+bool deposit_binned(const pic_grid *g, const void *ws, int64_t ws_bytes, int64_t most);
+// The end of the next launch pair's steps from s0: at most kBinSteps of them
+// with tracks (*n_dep), kBinTracks tracks and kBinSpan steps.
+int64_t next_deposit_group(const int64_t *off, int64_t s0, int64_t n_steps, int64_t *n_dep);
+// The binned deposition of steps s0 .. s1 - 1 (tracks xs/ys[off[s] ..
+// off[s + 1]), a group of next_deposit_group) into targets[k] for the k-th
+// step with tracks, or with targets null into the workspace's pair buffers:
+// dens[s - s0] is step s's pairs, or null for a step without tracks.
+int launch_deposit_steps(const pic_grid *g, const double *xs, const double *ys, const int64_t *off, int64_t s0,
+                         int64_t s1, uint32_t *counts, void *ws, void *const *targets, const void **dens,
+                         cudaStream_t st);
+// Kernel launches issued by this library so far (every launch site reports
+// to check_launch; a captured graph's launches count at each replay).
+void count_launches(int64_t n);using BatchLaunch = pic_batch_launch;
 int batched_workspace_bytes(int32_t n_blocks, int32_t n_cfgs, int64_t *bytes);
 int batched_loop(const BatchLaunch &L, cudaStream_t st);
 int batched_persistent(const BatchLaunch &L, const int64_t *step_task_off, const int64_t *step_tracks,

@@ -57,9 +57,10 @@ def test_binding_covers_the_header(lib):
 
 
 def test_host_only_calls_without_a_gpu(lib):
-    assert lib.pic_abi_version() == 6
+    assert lib.pic_abi_version() == 7
     native = __import__("importlib").import_module(pkg().__name__ + "._native")
-    assert native.ABI_VERSION == 6
+    assert native.ABI_VERSION == 7
+    assert lib.pic_kernel_launches() == 0  # nothing launched without a GPU
     assert ctypes.sizeof(native.PicGrid) == 200  # 5 int64, 14 double, 11 int32, padded to 8
     assert lib.pic_kpitch(406) == 408
     assert lib.pic_kpitch(408) == 408
@@ -69,10 +70,10 @@ def test_host_only_calls_without_a_gpu(lib):
 
 def test_step_workspace_holds_the_track_lists_of_the_binned_deposition(lib):
     """The fixed part (tally partials of 152 x 32 blocks, counter, status)
-    plus, for no_xy <= 4096 and truncation boxes of at most 64 cells, a count
-    per 62 x 62-cell tile (padded to 256 bytes), 4096 track indices per tile,
-    and the boxes (4 int16) and factors (2 x 64 of the field type) of 16384
-    tracks."""
+    plus, for no_xy <= 4096 and truncation boxes of at most 64 cells, for
+    each of 8 steps a count per 62 x 62-cell tile (padded to 256 bytes) and
+    4096 track indices per tile, the boxes (4 int16) and factors (2 x 64 of
+    the field type) of 65536 tracks, and 8 steps' deposition pairs."""
     import importlib
 
     P = pkg()
@@ -87,7 +88,9 @@ def test_step_workspace_holds_the_track_lists_of_the_binned_deposition(lib):
         b = ctypes.c_int64()
         assert lib.pic_step_workspace_bytes(ctypes.byref(g), ctypes.byref(b)) == 0
         tiles = ((n + 61) // 62) ** 2
-        assert b.value == fixed + (4 * tiles + 255) // 256 * 256 + tiles * 4096 * 4 + 16384 * 8 + 16384 * 128 * 4
+        pairs = (n * ((n + 3) // 4 * 4) * 2 * 4 + 255) // 256 * 256
+        assert b.value == (fixed + (8 * 4 * tiles + 255) // 256 * 256 + 8 * tiles * 4096 * 4 + 65536 * 8
+                           + 65536 * 128 * 4 + 8 * pairs)
     assert E.apply_shape(g, {"deposit_variant": "binned"}).deposit_variant == 2
     with pytest.raises(ValueError):
         E.apply_shape(g, {"deposit_variant": "tiles"})

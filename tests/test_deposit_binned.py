@@ -179,3 +179,132 @@ def test_pic_deposit_refuses_the_binned_form():
     rc = lib.pic_deposit(ctypes.byref(g), ctypes.c_void_p(xs.data_ptr()), ctypes.c_void_p(xs.data_ptr()), 1,
                          ctypes.c_void_p(dens.data_ptr()), ctypes.c_void_p(counts.data_ptr()), 0)
     assert rc == N.PIC_E_INVALID and b"binned deposition needs the step workspace" in lib.pic_last_error()
+
+
+# ------------------------------------------- segments: eight steps per launch
+
+
+def _thin_config(grid):
+    """The grid's lateral size with a 0.02 cm gap (46 k-planes), so that
+    float64 segments of a 328 x 328 grid stay small and quick."""
+    P, _, _ = _mods()
+    um, r = GRIDS[grid]
+    return P.SimulationConfig(**dict(BEAM, electrode_gap_cm=0.02, voltage_V=30.0, grid_size_um=um,
+                                     sampled_radius_cm=r, seed=1, max_voxels=2e9))
+
+
+def _segment_tracks(n, counts, seed):
+    rng = np.random.default_rng(seed)
+    m = int(sum(counts))
+    off = np.zeros(len(counts) + 1, dtype=np.int64)
+    np.cumsum(counts, out=off[1:])
+    return rng.uniform(0.0, n, m), rng.uniform(0.0, n, m), off
+
+
+def _groups(counts, steps=8, tracks=65536, span=256):
+    """Launch pairs of the segment loop: greedy groups of at most `steps`
+    depositing steps, `tracks` tracks and `span` steps."""
+    groups, s, n = 0, 0, len(counts)
+    while s < n:
+        e, nd, tr = s, 0, 0
+        while e < n and e - s < span:
+            if counts[e] > 0 and (nd == steps or tr + counts[e] > tracks):
+                break
+            nd += counts[e] > 0
+            tr += counts[e]
+            e += 1
+        groups += nd > 0
+        s = e
+    return groups
+
+
+def _run(cfg, xs, ys, off, dtype, variant, graphed=False):
+    import torch
+
+    _, E, N = _mods()
+    lib = N.load()
+    eng = E.ChamberEngine(cfg, dtype=dtype, max_tracks=len(xs), tally_steps=len(off) - 1,
+                          shape={"deposit_variant": variant})
+    try:
+        eng.upload_tracks(xs, ys, non_blocking=False)
+        torch.cuda.synchronize()
+        l0 = lib.pic_kernel_launches()
+        if graphed:
+            eng.run_segment_graphed("all", off)
+        else:
+            eng.run_segment(off)
+        torch.cuda.synchronize()
+        launches = lib.pic_kernel_launches() - l0
+        n = int(cfg.no_xy)
+        pos, neg = eng.fields()
+        dens = [d.view(n, -1, 2)[:, :n].cpu().numpy().astype(np.float64) for d in eng.dens]
+        return dict(tally=eng.tallies(len(off) - 1).copy(), pos=pos, neg=neg, dens=dens,
+                    counts=eng.counts.cpu().numpy().copy(), launches=launches)
+    finally:
+        eng.close()
+
+
+# per-step track counts: depositing and idle steps mixed, a long idle stretch,
+# steps that fill a launch's eight slots and one that crosses its track limit
+SEGMENT = [300, 0, 0, 500, 20, 0, 1, 700, 700, 700, 700, 700, 700, 700, 700, 700, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
+           0, 0, 40000, 30000, 5, 0, 9]
+
+
+@pytest.mark.parametrize("dtype, tol", [("float64", 1e-12), ("float32", 1e-6)])
+def test_a_segment_deposits_up_to_eight_steps_per_launch_pair(dtype, tol):
+    cfg = _thin_config("n328")
+    n = int(cfg.no_xy)
+    xs, ys, off = _segment_tracks(n, SEGMENT, seed=3)
+    a = _run(cfg, xs, ys, off, dtype, "binned")
+    b = _run(cfg, xs, ys, off, dtype, "tracks")
+    for k in range(4):
+        np.testing.assert_allclose(a["tally"][:, k], b["tally"][:, k], rtol=0, atol=tol * np.abs(b["tally"][:, k]).max())
+    peak = np.abs(b["pos"]).max()
+    np.testing.assert_allclose(a["pos"], b["pos"], rtol=0, atol=tol * peak)
+    np.testing.assert_allclose(a["neg"], b["neg"], rtol=0, atol=tol * peak)
+    np.testing.assert_array_equal(a["counts"], b["counts"])
+    # the caller's buffers: the last step's pairs, the other one zero
+    last = (len(SEGMENT) - 1) & 1
+    _close(a["dens"][last], b["dens"][last][..., 0], b["dens"][last][..., 1], tol)
+    assert not a["dens"][last ^ 1].any() and not b["dens"][last ^ 1].any()
+    steps = len(SEGMENT)
+    assert a["launches"] == steps + 2 * _groups(SEGMENT)
+    assert b["launches"] == steps + sum(c > 0 for c in SEGMENT)
+
+
+def test_a_segment_with_a_step_beyond_the_launch_limit_deposits_step_by_step():
+    """A step of more than 65536 tracks: the segment deposits one step at a
+    time, that step in two pieces (the second adds to the first)."""
+    cfg = _thin_config("n328")
+    n = int(cfg.no_xy)
+    counts = [100, 70000, 0, 50]
+    xs, ys, off = _segment_tracks(n, counts, seed=4)
+    a = _run(cfg, xs, ys, off, "float64", "binned")
+    b = _run(cfg, xs, ys, off, "float64", "tracks")
+    np.testing.assert_allclose(a["tally"], b["tally"], rtol=1e-12, atol=0)
+    np.testing.assert_allclose(a["pos"], b["pos"], rtol=0, atol=1e-12 * np.abs(b["pos"]).max())
+    assert a["launches"] == len(counts) + 2 * (1 + 2 + 1)  # two launches a piece
+
+
+def test_graph_replays_of_a_binned_segment_repeat_the_direct_run_bit_for_bit():
+    cfg = _thin_config("n328")
+    n = int(cfg.no_xy)
+    xs, ys, off = _segment_tracks(n, SEGMENT, seed=5)
+    a = _run(cfg, xs, ys, off, "float32", "binned")
+    g = _run(cfg, xs, ys, off, "float32", "binned", graphed=True)
+    np.testing.assert_array_equal(g["tally"], a["tally"])
+    np.testing.assert_array_equal(g["pos"], a["pos"])
+    assert g["launches"] == a["launches"]  # a replay counts the launches captured into it
+
+
+@pytest.mark.parametrize("dtype, tol", [("float64", 1e-10), ("float32", 1e-5)])
+def test_the_gradients_forward_pass_deposits_in_groups_into_its_kept_slots(dtype, tol):
+    """pic_adjoint_forward with the binned form deposits up to eight steps
+    per launch pair straight into the slots it keeps for the reverse sweep:
+    k_s and the whole gradient equal the per-track form's."""
+    A = importlib.import_module(pkg().__name__ + ".adjoint")
+    cfg = _config("n24")
+    ks_b, g_b, _ = A.ks_and_gradient(cfg, None, dtype=dtype, shape={"deposit_variant": "binned"})
+    ks_t, g_t, _ = A.ks_and_gradient(cfg, None, dtype=dtype, shape={"deposit_variant": "tracks"})
+    assert ks_b == pytest.approx(ks_t, rel=tol)
+    np.testing.assert_allclose(g_b, g_t, rtol=tol, atol=0)
