@@ -208,14 +208,15 @@ def _phases(total_steps: Sequence[int]):
 
 
 DEP_TILE = 64  # cells per side of a deposition tile (pic_deposit.cuh, kDepTile)
+DEP_PART_TRACKS = 32  # tracks per part of a tile (pic_deposit.cuh, kDepPartTracks)
 
 
 def deposit_blocks(no_xy, tracks):
     """Blocks of the tile-form deposition of one grid's tracks in one step:
-    tiles x parts, parts = one per 32 tracks, 1 to 32 (pic_deposit.cuh,
-    deposit_tiles / deposit_tile_parts)."""
+    tiles x parts, parts = one per DEP_PART_TRACKS tracks, 1 to 32
+    (pic_deposit.cuh, deposit_tiles / deposit_tile_parts)."""
     tiles = (-(-np.asarray(no_xy, dtype=np.int64) // DEP_TILE)) ** 2
-    parts = np.clip(-(-np.asarray(tracks, dtype=np.int64) // 32), 1, 32)
+    parts = np.clip(-(-np.asarray(tracks, dtype=np.int64) // DEP_PART_TRACKS), 1, 32)
     return tiles * parts
 
 
