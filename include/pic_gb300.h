@@ -492,10 +492,30 @@ typedef struct pic_batch_launch {
     double *tally;                         /* device, packed [rows][4] tallies               */
     void *workspace;                       /* device, pic_batched_workspace_bytes, zeroed    */
     int64_t workspace_bytes;
+    /* The binned deposition (every grid's tracks listed per 62 x 62-cell
+     * tile, summed by one block per tile in a fixed order, each cell stored
+     * once), up to 8 global steps per pair of launches, each step's pairs in
+     * a buffer of the deposition workspace (pic_batched_segment; the
+     * streaming step deposits one global step at a time into dens). With
+     * dep_workspace null: the tile form (step_blocks). Needs n_cfgs <= 1024
+     * and every grid's cutoff_voxels < 31.5 (boxes of at most 64 cells). */
+    void *dep_workspace;                   /* device, pic_batched_deposit_bytes, zeroed once */
+    int64_t dep_workspace_bytes;
+    int64_t dep_max_tracks;                /* the most tracks of 8 consecutive global steps  */
+    int64_t dep_dens_bytes;                /* bytes of one packed pair buffer (dens[0])      */
+    int32_t dep_total_tiles;               /* sum over the grids of ceil(no_xy / 62)^2       */
+    int32_t dep_max_tiles;                 /* the largest of those                           */
 } pic_batch_launch;
 
 /* Workspace of a batched launch with n_blocks blocks and n_cfgs grids. */
 int pic_batched_workspace_bytes(int32_t n_blocks, int32_t n_cfgs, int64_t *bytes);
+
+/* Workspace of the binned batched deposition: for each of 8 steps a slot
+ * per grid, the per-tile track counts and lists of total_tiles tiles and a
+ * packed pair buffer of dens_bytes; the boxes and factors of max_tracks
+ * tracks in the field type (dtype). */
+int pic_batched_deposit_bytes(int32_t n_cfgs, int32_t total_tiles, int64_t max_tracks, int64_t dens_bytes,
+                              int32_t dtype, int64_t *bytes);
 
 /* Runs global steps [first_step, first_step + n_steps) of a batch. Step s
  * reads time level s & 1 and density buffer s & 1, writes level (s+1) & 1

@@ -27,7 +27,7 @@ PIC_DEPOSIT_AUTO = 0
 PIC_DEPOSIT_TRACKS = 1
 PIC_DEPOSIT_BINNED = 2
 # pic_abi_version() of the library these structures mirror
-ABI_VERSION = 7
+ABI_VERSION = 8
 
 _LIB_PATH = Path(__file__).resolve().parent / "_build" / "libpic_gb300.so"
 _lock = threading.Lock()
@@ -185,6 +185,8 @@ EXPORTS = {
          ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)],
     ),
     "pic_batched_workspace_bytes": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]),
+    "pic_batched_deposit_bytes": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64,
+                                                 ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]),
     "pic_batched_segment": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "pic_batched_graph_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
     "pic_batched_stream_workspace_bytes": (

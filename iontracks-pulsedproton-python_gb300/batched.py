@@ -160,7 +160,30 @@ class PicBatchLaunch(ctypes.Structure):
         ("tally", ctypes.c_void_p),
         ("workspace", ctypes.c_void_p),
         ("workspace_bytes", ctypes.c_int64),
+        ("dep_workspace", ctypes.c_void_p),
+        ("dep_workspace_bytes", ctypes.c_int64),
+        ("dep_max_tracks", ctypes.c_int64),
+        ("dep_dens_bytes", ctypes.c_int64),
+        ("dep_total_tiles", ctypes.c_int32),
+        ("dep_max_tiles", ctypes.c_int32),
     ]
+
+
+BIN_OUT = 62  # output cells per side of a binned deposition tile (pic_internal.h, kBinOut)
+BIN_MAX_SLOTS = 1024  # grids the binned batched deposition takes (kBinMaxSlots)
+BIN_STEPS = 8  # global steps per binned deposition launch pair (kBinSteps)
+
+
+def binned_tiles(no_xy):
+    """62 x 62-cell tiles of the binned deposition of grids of side no_xy."""
+    return (-(-np.asarray(no_xy, dtype=np.int64) // BIN_OUT)) ** 2
+
+
+def binned_eligible(grids) -> bool:
+    """Whether the binned batched deposition takes these grids: at most 1024,
+    each no_xy <= 4096 with truncation boxes of at most 64 cells."""
+    return len(grids) <= BIN_MAX_SLOTS and all(
+        int(g.no_xy) <= 4096 and 2.0 * float(g.cutoff_voxels) + 1.0 < 64.0 for g in grids)
 
 
 def _align(x: int, a: int = 64) -> int:
@@ -285,6 +308,7 @@ def run_batched_b200(
     solo_grids: int = SOLO_MAX_GRIDS,
     variant: str = "auto",
     escalate: bool = True,
+    deposit: str = "auto",
 ):
     """Simulate every configuration and return their Results, in order.
 
@@ -307,6 +331,11 @@ def run_batched_b200(
     ``escalate``: a float32 configuration whose tallies come back non-finite
     is run again alone with float64 fields from the same generator state
     (run_simulation_b200's ``escalate``), and that Result takes its place.
+    ``deposit`` picks the deposition of the batched launches: "binned" (every
+    grid's tracks of a global step listed per 62 x 62-cell tile and summed by
+    one block per tile, each cell stored once), "tiles" (a block per tile and
+    32-track part, adding with atomics), or "auto" (binned where the grids
+    allow it, ``binned_eligible``).
     """
     import torch
 
@@ -321,6 +350,8 @@ def run_batched_b200(
         raise ValueError("solo_grids must be >= 0")
     if variant not in ("auto", "flat", "stream"):
         raise ValueError(f"variant must be 'auto', 'flat' or 'stream', got {variant!r}")
+    if deposit not in ("auto", "binned", "tiles"):
+        raise ValueError(f"deposit must be 'auto', 'binned' or 'tiles', got {deposit!r}")
     if variant == "stream" and (dtype != "float32" or persistent):
         raise ValueError("the streaming batched step takes float32 batches without persistent launches")
     if not torch.cuda.is_available():
@@ -399,6 +430,22 @@ def run_batched_b200(
     task_cfg = one(t_cfg, np.int32)
     task_first = one(t_first, np.int64)
     task_prefix = one(t_prefix, np.int64)
+    binned = deposit == "binned" or (deposit == "auto" and binned_eligible(grids))
+    if binned and not binned_eligible(grids):
+        raise ValueError("the binned deposition takes at most 1024 grids, each no_xy <= 4096 with cutoff < 31.5 voxels")
+    dep_ws, dep_tiles, dep_max_tiles, dep_max_tracks, dep_dens_bytes = None, 0, 0, 0, 0
+    if binned and not persistent:
+        tiles_c = binned_tiles([int(g.no_xy) for g in grids])
+        dep_tiles, dep_max_tiles = int(tiles_c.sum()), int(tiles_c.max())
+        # the most tracks of BIN_STEPS consecutive global steps (one launch pair's)
+        window = np.convolve(np.asarray(step_tracks, dtype=np.int64), np.ones(BIN_STEPS, dtype=np.int64))
+        dep_max_tracks = int(window.max()) if len(window) else 0
+        dep_dens_bytes = int(dens[0].numel()) * dens[0].element_size()
+        dwb = ctypes.c_int64()
+        N.check(lib.pic_batched_deposit_bytes(n_cfg, dep_tiles, dep_max_tracks, dep_dens_bytes,
+                                              N.PIC_F32 if dtype == "float32" else N.PIC_F64, ctypes.byref(dwb)),
+                "pic_batched_deposit_bytes")
+        dep_ws = torch.zeros(int(dwb.value), dtype=torch.uint8, device=dev)
 
     # --- work tables, one per set of active grids
     phases = []
@@ -437,9 +484,12 @@ def run_batched_b200(
             stream_tabs[s0] = (bs, sws)
     solo_ws = None
     if solo_grids > 0 and not persistent and any(len(t["active"]) <= solo_grids for _, _, t in phases):
-        swb = ctypes.c_int64()
-        N.check(lib.pic_step_workspace_bytes(ctypes.byref(grids[0]), ctypes.byref(swb)), "pic_step_workspace_bytes")
-        solo_ws = torch.zeros(int(swb.value), dtype=torch.uint8, device=dev)
+        need = 0
+        for g in grids:  # one workspace for every solo grid: the largest any of them needs
+            swb = ctypes.c_int64()
+            N.check(lib.pic_step_workspace_bytes(ctypes.byref(g), ctypes.byref(swb)), "pic_step_workspace_bytes")
+            need = max(need, int(swb.value))
+        solo_ws = torch.zeros(need, dtype=torch.uint8, device=dev)
 
     solo_graphs = []  # graph handles, freed once the run has finished
 
@@ -564,6 +614,10 @@ def run_batched_b200(
             L.first_step, L.n_steps = c0, c1 - c0
             L.counts, L.tally = counts.data_ptr(), tally.data_ptr()
             L.workspace, L.workspace_bytes = workspace.data_ptr(), workspace.numel()
+            if dep_ws is not None:
+                L.dep_workspace, L.dep_workspace_bytes = dep_ws.data_ptr(), dep_ws.numel()
+                L.dep_max_tracks, L.dep_total_tiles, L.dep_max_tiles = dep_max_tracks, dep_tiles, dep_max_tiles
+                L.dep_dens_bytes = dep_dens_bytes
             with nvtx_range(f"batched steps ({len(tab['active'])} grids)"):
                 if tab["phase_start"] in stream_tabs:
                     bs = stream_tabs[tab["phase_start"]][0]

@@ -20,6 +20,7 @@
 #include <math.h>
 #include <stdint.h>
 
+#include "pic_binned.cuh"
 #include "pic_deposit.cuh"
 #include "pic_device.cuh"
 #include "pic_barrier.cuh"
@@ -47,7 +48,7 @@ struct BatchStepArgs {
     const T *pos_in, *neg_in;
     T *pos_out, *neg_out;
     const pair_t<T> *dens;  // packed deposition pairs of this step
-    pair_t<T> *dens_zero;   // packed pairs of the next step, cleared here
+    pair_t<T> *dens_zero;   // packed pairs of the next step, cleared here (null: none)
     double *tally;    // packed [rows][4]
     double *partials; // [n_blocks][4]
     unsigned int *counters;  // [n_cfgs]
@@ -137,7 +138,7 @@ __device__ __forceinline__ void batched_step_block(const BatchStepArgs<T> &b, in
             a.pos_out = b.pos_out + E->field_off;
             a.neg_out = b.neg_out + E->field_off;
             a.dens = b.dens + E->dens_off;
-            a.dens_zero = b.dens_zero + E->dens_off;
+            a.dens_zero = b.dens_zero ? b.dens_zero + E->dens_off : nullptr;  // null: nothing to clear
         }
     }
     __syncthreads();
@@ -414,12 +415,169 @@ int batched_status(const BatchLaunch &L, cudaStream_t st, int32_t *status) {
 
 template <typename T, typename I>
 static void launch_batched_step(const BatchLaunch &L, int bi, int bo, double *partials, unsigned int *counters,
-                                int64_t step, cudaStream_t st) {
+                                int64_t step, cudaStream_t st, const void *dens, void *dens_zero) {
     constexpr int BLOCK = 256;
     BatchStepArgs<T> b{L.cfgs, table_of<T>(L), L.blk_cfg, L.blk_item0, L.blk_item1, L.cfg_blk0, L.cfg_nblk,
                        (const T *)L.pos[bi], (const T *)L.neg[bi], (T *)L.pos[bo], (T *)L.neg[bo],
-                       (const pair_t<T> *)L.dens[bi], (pair_t<T> *)L.dens[bo], L.tally, partials, counters, step};
+                       (const pair_t<T> *)dens, (pair_t<T> *)dens_zero, L.tally, partials, counters, step};
     batched_step_kernel<T, BLOCK, I><<<(unsigned)L.n_blocks, BLOCK, 0, st>>>(b);
+}
+
+// ---------------------------------------------------------------------------
+// The binned deposition (pic_binned.cuh) of up to kBinSteps global steps per
+// launch pair: a slot per task (a grid with tracks in a step), built on the
+// device by batched_bin_prep_kernel from the task list and the grid table,
+// then the binning and tile launches over those slots. Step q of a group
+// writes its pairs into the q-th packed pair buffer of the workspace (zeroed
+// first), which its batched step then reads. Workspace layout: [slots,
+// kBinSteps x n_cfgs, padded to 256 bytes | per-tile counts, kBinSteps x
+// total_tiles ints, padded | per-tile lists, kBinSteps x total_tiles x
+// kBinCap ints | boxes, max_tracks short4, padded | factors, max_tracks x 2 x
+// kBinBox of the field type, padded | kBinSteps packed pair buffers, each
+// dens_bytes padded to 256].
+static int64_t pad256(int64_t b) { return (b + 255) / 256 * 256; }
+
+int64_t batched_deposit_bytes(int32_t n_cfgs, int32_t total_tiles, int64_t max_tracks, int64_t dens_bytes,
+                              int32_t dtype) {
+    const int64_t es = dtype == PIC_F64 ? 8 : 4;
+    const int64_t slot = dtype == PIC_F64 ? (int64_t)sizeof(BinSlot<double>) : (int64_t)sizeof(BinSlot<float>);
+    const int64_t tiles = (int64_t)kBinSteps * total_tiles;
+    return pad256(kBinSteps * n_cfgs * slot) + pad256(tiles * 4) + tiles * kBinCap * 4 + pad256(max_tracks * 8) +
+           pad256(max_tracks * 2 * kBinBox * es) + kBinSteps * pad256(dens_bytes);
+}
+
+template <typename T>
+struct BatchedBins {
+    BinSlot<T> *slots;
+    int *count, *list;
+    BinScratch<T> sc;
+    char *dens;  // kBinSteps packed pair buffers
+    int64_t dens_stride;
+};
+template <typename T>
+static BatchedBins<T> batched_bins(const BatchLaunch &L) {
+    const int64_t tiles = (int64_t)kBinSteps * L.dep_total_tiles;
+    char *b = static_cast<char *>(L.dep_workspace);
+    char *count = b + pad256((int64_t)kBinSteps * L.n_cfgs * sizeof(BinSlot<T>));
+    char *list = count + pad256(tiles * 4);
+    char *box = list + tiles * kBinCap * 4;
+    char *fac = box + pad256(L.dep_max_tracks * 8);
+    char *dens = fac + pad256(L.dep_max_tracks * 2 * kBinBox * (int64_t)sizeof(T));
+    return BatchedBins<T>{reinterpret_cast<BinSlot<T> *>(b), reinterpret_cast<int *>(count),
+                          reinterpret_cast<int *>(list),
+                          BinScratch<T>{reinterpret_cast<short4 *>(box), reinterpret_cast<T *>(fac)}, dens,
+                          pad256(L.dep_dens_bytes)};
+}
+
+// The steps of one group, by value: step q's tasks are [task_off[q],
+// task_off[q + 1]) of the group's (counted from its first task), its tracks
+// start at launch track track_base[q], its pairs go to dens[q].
+template <typename T>
+struct BinGroup {
+    int64_t task_off[kBinSteps + 1];
+    int64_t track_base[kBinSteps + 1];
+    pair_t<T> *dens[kBinSteps];
+    int steps;
+};
+
+// Task t's slot (its grid's scalars, tracks, pairs and histogram); the
+// tiles before it, a block-wide prefix sum carried over chunks of the block's
+// size, place its counts, lists and blocks.
+template <typename T>
+__global__ void __launch_bounds__(kBinMaxSlots) batched_bin_prep_kernel(
+    const pic_batch_cfg *cfgs, const int32_t *task_cfg, const int64_t *task_first, const int64_t *task_prefix,
+    int n_tasks, BinGroup<T> G, const double *xs, const double *ys, uint32_t *counts, int *count_base,
+    int *list_base, BinSlot<T> *out) {
+    __shared__ int64_t pre[kBinMaxSlots];
+    __shared__ int64_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    for (int c0 = 0; c0 < n_tasks; c0 += blockDim.x) {
+        const int t = c0 + (int)threadIdx.x;
+        BinSlot<T> s{};
+        int64_t tiles = 0;
+        if (t < n_tasks) {
+            int q = 0;
+            while (q + 1 < G.steps && G.task_off[q + 1] <= t) ++q;
+            const pic_batch_cfg &C = cfgs[task_cfg[t]];
+            const pic_grid &g = C.grid;
+            const int n = (int)g.no_xy;
+            s.xs = xs + task_first[t];
+            s.ys = ys + task_first[t];
+            s.dens = G.dens[q] + C.dens_off;
+            s.hist = counts + C.counts_off;
+            s.first = G.track_base[q] + task_prefix[t];
+            s.last = t + 1 < G.task_off[q + 1] ? G.track_base[q] + task_prefix[t + 1] : G.track_base[q + 1];
+            s.cut = g.cutoff_voxels;
+            s.h2b2 = (T)g.h2_over_b2;
+            s.gfac = (T)g.gaussian_factor;
+            s.n = n;
+            s.dp = (n + 3) / 4 * 4;
+            s.tps = (n + kBinOut - 1) / kBinOut;
+            s.add = 0;
+            tiles = (int64_t)s.tps * s.tps;
+        }
+        pre[threadIdx.x] = tiles;
+        __syncthreads();
+        for (int d = 1; d < (int)blockDim.x; d <<= 1) {
+            const int64_t v = (int)threadIdx.x >= d ? pre[threadIdx.x - d] : 0;
+            __syncthreads();
+            pre[threadIdx.x] += v;
+            __syncthreads();
+        }
+        if (t < n_tasks) {
+            const int64_t base = carry + pre[threadIdx.x] - tiles;
+            s.count = count_base + base;
+            s.list = list_base + base * kBinCap;
+            s.block0 = (int32_t)base;
+            out[t] = s;
+        }
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry += pre[threadIdx.x];
+        __syncthreads();
+    }
+}
+
+// Global steps s0 .. s1 - 1 of the launch (at most kBinSteps, their tracks
+// within dep_max_tracks) deposited together. pairs[s - s0]: step s's pairs
+// (a zeroed workspace buffer holding its tracks), or null for a step
+// without tracks. With to_dens, one step into the launch's own dens[bi]
+// instead (the streaming batched step).
+template <typename T>
+static int batched_binned_deposit(const BatchLaunch &L, int64_t s0, int64_t s1, const void **pairs, int to_dens,
+                                  cudaStream_t st) {
+    const BatchedBins<T> B = batched_bins<T>(L);
+    BinGroup<T> G{};
+    const int64_t t0 = L.step_task_off[s0];
+    int64_t tracks = 0;
+    G.steps = (int)(s1 - s0);
+    for (int q = 0; q < G.steps; ++q) {
+        const int64_t s = s0 + q;
+        G.task_off[q] = L.step_task_off[s] - t0;
+        G.track_base[q] = tracks;
+        const bool dep = L.step_tracks[s] > 0 && L.step_task_off[s + 1] > L.step_task_off[s];
+        if (to_dens) {
+            G.dens[q] = static_cast<pair_t<T> *>(L.dens[(L.first_step + s) & 1]);
+        } else {
+            G.dens[q] = reinterpret_cast<pair_t<T> *>(B.dens + q * B.dens_stride);
+            if (dep) {
+                cudaError_t e = cudaMemsetAsync(G.dens[q], 0, (size_t)L.dep_dens_bytes, st);
+                if (e != cudaSuccess) return set_cuda_error("cudaMemsetAsync(batched deposition pairs)", e);
+            }
+        }
+        pairs[q] = dep ? G.dens[q] : nullptr;
+        tracks += dep ? L.step_tracks[s] : 0;
+    }
+    G.task_off[G.steps] = L.step_task_off[s1] - t0;
+    G.track_base[G.steps] = tracks;
+    const int nt = (int)(L.step_task_off[s1] - t0);
+    if (nt == 0 || tracks == 0) return PIC_OK;
+    batched_bin_prep_kernel<T><<<1, nt < kBinMaxSlots ? (nt + 31) / 32 * 32 : kBinMaxSlots, 0, st>>>(
+        L.cfgs, L.task_cfg + t0, L.task_first + t0, L.task_prefix + t0, nt, G, L.xs, L.ys, L.counts, B.count,
+        B.list, B.slots);
+    int rc = check_launch("batched_bin_prep_kernel");
+    if (rc) return rc;
+    const BinSlotsDevice<T> S{B.slots, nt, tracks};
+    return binned_launches<T>(S, B.sc, (int64_t)nt * L.dep_max_tiles, st);
 }
 
 int batched_loop(const BatchLaunch &L, cudaStream_t st) { return batched_loop_stream(L, nullptr, st); }
@@ -431,12 +589,51 @@ int batched_loop_stream(const BatchLaunch &L, const pic_batch_stream *B, cudaStr
         int rc = L.dtype == PIC_F64 ? prep_table<double>(L, st) : prep_table<float>(L, st);
         if (rc) return rc;
     }
+    auto step_launch = [&](int64_t step, int bi, int bo, const void *dens, void *dens_zero) {
+        if (L.dtype == PIC_F64) {
+            if (L.index32) launch_batched_step<double, uint32_t>(L, bi, bo, partials, counters, step, st, dens, dens_zero);
+            else launch_batched_step<double, int64_t>(L, bi, bo, partials, counters, step, st, dens, dens_zero);
+        } else {
+            if (L.index32) launch_batched_step<float, uint32_t>(L, bi, bo, partials, counters, step, st, dens, dens_zero);
+            else launch_batched_step<float, int64_t>(L, bi, bo, partials, counters, step, st, dens, dens_zero);
+        }
+        return check_launch("batched_step_kernel");
+    };
+    if (L.dep_workspace && !B) {
+        // groups of up to kBinSteps global steps (dep_max_tracks tracks):
+        // their binned deposition into the workspace's pair buffers, then
+        // their steps, which read those buffers (no pairs to clear: the
+        // launch's own dens buffers stay zero)
+        const void *pairs[kBinSteps];
+        for (int64_t s0 = 0; s0 < L.n_steps;) {
+            int64_t s1 = s0, tr = 0;
+            while (s1 < L.n_steps && s1 - s0 < kBinSteps && tr + L.step_tracks[s1] <= L.dep_max_tracks)
+                tr += L.step_tracks[s1++];
+            if (s1 == s0) return set_error(PIC_E_INVALID, "a global step has more tracks than dep_max_tracks");
+            int rc = L.dtype == PIC_F64 ? batched_binned_deposit<double>(L, s0, s1, pairs, 0, st)
+                                        : batched_binned_deposit<float>(L, s0, s1, pairs, 0, st);
+            if (rc) return rc;
+            for (int64_t s = s0; s < s1; ++s) {
+                const int64_t step = L.first_step + s;
+                const int bi = (int)(step & 1);
+                if ((rc = step_launch(step, bi, bi ^ 1, pairs[s - s0] ? pairs[s - s0] : L.dens[bi], nullptr)))
+                    return rc;
+            }
+            s0 = s1;
+        }
+        return PIC_OK;
+    }
     for (int64_t s = 0; s < L.n_steps; ++s) {
         const int64_t step = L.first_step + s;
         const int bi = (int)(step & 1), bo = bi ^ 1;
         const int64_t t0 = L.step_task_off[s], t1 = L.step_task_off[s + 1];
         const int64_t tracks = L.step_tracks[s];
-        if (tracks > 0 && t1 > t0) {
+        if (tracks > 0 && t1 > t0 && L.dep_workspace) {
+            const void *pairs[1];
+            int rc = L.dtype == PIC_F64 ? batched_binned_deposit<double>(L, s, s + 1, pairs, 1, st)
+                                        : batched_binned_deposit<float>(L, s, s + 1, pairs, 1, st);
+            if (rc) return rc;
+        } else if (tracks > 0 && t1 > t0) {
             const unsigned blocks = (unsigned)L.step_blocks[s];
             if (L.dtype == PIC_F64)
                 batched_deposit_kernel<double><<<blocks, kDepThreads, 0, st>>>(
@@ -454,14 +651,7 @@ int batched_loop_stream(const BatchLaunch &L, const pic_batch_stream *B, cudaStr
             if (rc) return rc;
             continue;
         }
-        if (L.dtype == PIC_F64) {
-            if (L.index32) launch_batched_step<double, uint32_t>(L, bi, bo, partials, counters, step, st);
-            else launch_batched_step<double, int64_t>(L, bi, bo, partials, counters, step, st);
-        } else {
-            if (L.index32) launch_batched_step<float, uint32_t>(L, bi, bo, partials, counters, step, st);
-            else launch_batched_step<float, int64_t>(L, bi, bo, partials, counters, step, st);
-        }
-        int rc = check_launch("batched_step_kernel");
+        int rc = step_launch(step, bi, bo, L.dens[bi], L.dens[bo]);
         if (rc) return rc;
     }
     return PIC_OK;

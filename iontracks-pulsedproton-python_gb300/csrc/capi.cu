@@ -308,8 +308,22 @@ static int check_batch_common(const pic_batch_launch *L) {
             return set_error(PIC_E_INVALID, "step task offsets must be non-decreasing");
         if (L->step_tracks[s] > 0 && (!L->task_cfg || !L->task_first || !L->task_prefix || !L->xs || !L->ys))
             return set_error(PIC_E_INVALID, "track or task arrays are null");
-        if (L->step_tracks[s] > 0 && (L->step_blocks[s] < 1 || L->step_blocks[s] > 0x7fffffffLL))
+        if (L->step_tracks[s] > 0 && !L->dep_workspace &&
+            (L->step_blocks[s] < 1 || L->step_blocks[s] > 0x7fffffffLL))
             return set_error(PIC_E_INVALID, "step_blocks must give each depositing step 1 .. 2^31-1 blocks");
+        if (L->dep_workspace && L->step_tracks[s] > L->dep_max_tracks)
+            return set_error(PIC_E_INVALID, "a global step has more tracks than dep_max_tracks");
+    }
+    if (L->dep_workspace) {
+        if (L->n_cfgs > kBinMaxSlots) return set_error(PIC_E_INVALID, "the binned batched deposition takes at most 1024 grids");
+        if (L->dep_total_tiles < 1 || L->dep_max_tiles < 1 || L->dep_max_tiles > L->dep_total_tiles ||
+            L->dep_max_tracks < 0 || L->dep_dens_bytes < 1)
+            return set_error(PIC_E_INVALID,
+                             "dep_total_tiles, dep_max_tiles, dep_max_tracks and dep_dens_bytes are inconsistent");
+        if (!aligned(L->dep_workspace, 256) ||
+            L->dep_workspace_bytes < batched_deposit_bytes(L->n_cfgs, L->dep_total_tiles, L->dep_max_tracks,
+                                                           L->dep_dens_bytes, L->dtype))
+            return set_error(PIC_E_INVALID, "dep_workspace too small or not 256-byte aligned (pic_batched_deposit_bytes)");
     }
     return PIC_OK;
 }
@@ -339,7 +353,7 @@ const char *pic_last_error(void) { return g_last_error.c_str(); }
 // double, 9 int32, padded to 8 bytes).
 static_assert(sizeof(pic_grid) == 200, "pic_grid layout changed: bump pic_abi_version and the bindings");
 
-int pic_abi_version(void) { return 7; }
+int pic_abi_version(void) { return 8; }
 
 int64_t pic_kpitch(int64_t nzb) { return (nzb + 7) / 8 * 8; }
 
@@ -833,6 +847,17 @@ int pic_capture_end(uintptr_t stream, uintptr_t *graph_out) {
 int pic_batched_workspace_bytes(int32_t n_blocks, int32_t n_cfgs, int64_t *bytes) {
     if (!bytes) return set_error(PIC_E_INVALID, "bytes is null");
     return batched_workspace_bytes(n_blocks, n_cfgs, bytes);
+}
+
+int pic_batched_deposit_bytes(int32_t n_cfgs, int32_t total_tiles, int64_t max_tracks, int64_t dens_bytes,
+                              int32_t dtype, int64_t *bytes) {
+    if (!bytes) return set_error(PIC_E_INVALID, "bytes is null");
+    if (n_cfgs < 1 || n_cfgs > kBinMaxSlots) return set_error(PIC_E_INVALID, "n_cfgs must be 1 .. 1024");
+    if (total_tiles < 1 || max_tracks < 0 || dens_bytes < 1)
+        return set_error(PIC_E_INVALID, "total_tiles >= 1, max_tracks >= 0 and dens_bytes >= 1");
+    if (dtype != PIC_F32 && dtype != PIC_F64) return set_error(PIC_E_INVALID, "dtype must be PIC_F32 or PIC_F64");
+    *bytes = batched_deposit_bytes(n_cfgs, total_tiles, max_tracks, dens_bytes, dtype);
+    return PIC_OK;
 }
 
 int pic_batched_segment(const pic_batch_launch *launch, uintptr_t stream) {

@@ -201,6 +201,12 @@ inline int64_t dep_bin_bytes(const pic_grid *g) {
     return bin_count_bytes(g->no_xy) + bin_list_bytes(g->no_xy) + bin_box_bytes() + bin_fac_bytes(es) +
            kBinSteps * bin_dens_bytes(g->no_xy, es);
 }
+// The binned deposition of a batched global step (batched.cu): its workspace
+// (a slot per grid, per-tile counts and lists, per-track boxes and factors).
+constexpr int kBinMaxSlots = 1024;
+int64_t batched_deposit_bytes(int32_t n_cfgs, int32_t total_tiles, int64_t max_tracks, int64_t dens_bytes,
+                              int32_t dtype);
+
 // Whether the deposition takes the binned form for this grid and workspace:
 // for a segment's steps together (most = the most tracks one of them has),
 // or with most < 0 for one step alone.

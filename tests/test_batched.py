@@ -358,3 +358,64 @@ def test_a_configuration_float32_cannot_follow_is_run_again_in_float64():
     assert easy.fields_dtype == "float32" and abs(easy.ks - fx[0]["ks"]) <= KS_ABS
     nan = pkg().run_simulation_b200(cfgs[27], progress=False, return_fields=False)
     assert nan.fields_dtype == "float64" and not np.isfinite(nan.ks)  # as in the reference
+
+
+# ------------------------------------------------ binned batched deposition
+
+
+def test_binned_batched_deposition_workspace_and_arguments():
+    """pic_batched_deposit_bytes: for each of 8 global steps a slot per grid,
+    per-tile counts and lists and a packed pair buffer; per-track boxes and
+    factors; the run's choices are checked before any device work."""
+    import ctypes
+    import importlib
+
+    P = pkg()
+    N = importlib.import_module(P.__name__ + "._native")
+    B = importlib.import_module(P.__name__ + ".batched")
+    lib = N.load()
+    b = ctypes.c_int64()
+    assert lib.pic_batched_deposit_bytes(64, 200, 248000, 3_300_000, N.PIC_F32, ctypes.byref(b)) == N.PIC_OK
+    pad = lambda x: (x + 255) // 256 * 256  # noqa: E731
+    rest = pad(8 * 200 * 4) + 8 * 200 * 4096 * 4 + pad(248000 * 8) + pad(248000 * 128 * 4) + 8 * pad(3_300_000)
+    slot = (b.value - rest) // (8 * 64)
+    assert 64 <= slot <= 128 and slot % 8 == 0  # one descriptor per grid and step of a launch pair
+    assert lib.pic_batched_deposit_bytes(1025, 200, 10, 8, N.PIC_F32, ctypes.byref(b)) == N.PIC_E_INVALID
+    assert lib.pic_batched_deposit_bytes(4, 0, 10, 8, N.PIC_F32, ctypes.byref(b)) == N.PIC_E_INVALID
+    assert lib.pic_batched_deposit_bytes(4, 4, 10, 0, N.PIC_F32, ctypes.byref(b)) == N.PIC_E_INVALID
+    assert lib.pic_batched_deposit_bytes(4, 4, 10, 8, 7, ctypes.byref(b)) == N.PIC_E_INVALID
+    np.testing.assert_array_equal(B.binned_tiles([24, 62, 63, 124, 1068]), [1, 1, 4, 4, 324])
+    grids = [type("G", (), dict(no_xy=n, cutoff_voxels=c))() for n, c in ((24, 14.1), (608, 28.3))]
+    assert B.binned_eligible(grids)
+    assert not B.binned_eligible(grids + [type("G", (), dict(no_xy=64, cutoff_voxels=31.6))()])
+    with pytest.raises(ValueError, match="deposit"):
+        B.run_batched_b200([make_config("fast")], deposit="atomic")
+
+
+@pytest.mark.gpu
+def test_binned_batched_deposition_matches_the_tile_form():
+    """Every grid's tracks of a global step listed per tile and summed by one
+    block per tile, against the tile form's atomics, on the mixed batch (both
+    walls, odd no_xy, the full-grid scoring region, two species) and eight
+    sweep grids: identical tracks, k_s and tallies within 1e-5, fields within
+    1e-5 of their peak; chunks of 7 global steps, the single-grid tail phases
+    off so that every step goes through the batched launches."""
+    cfgs = _mixed_batch() + [c for c in pkg().saturation_sweep_configs()
+                             if c.no_xy ** 2 * c.no_z_with_buffer < 1.5e6][:8]
+    a = pkg().run_batched_b200(cfgs, chunk_steps=7, solo_grids=0, deposit="tiles", return_fields=True)
+    b = pkg().run_batched_b200(cfgs, chunk_steps=7, solo_grids=0, deposit="binned", return_fields=True)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x.track_density_xy, y.track_density_xy)
+        assert abs(x.ks - y.ks) <= KS_ABS
+        np.testing.assert_allclose(y.recombination, x.recombination, rtol=0,
+                                   atol=1e-5 * max(np.abs(x.recombination).max(), 1e-300))
+        np.testing.assert_allclose(y.injected_positive, x.injected_positive, rtol=1e-5, atol=0)
+        peak = max(np.abs(x.positive_array).max(), 1e-300)
+        np.testing.assert_allclose(y.positive_array, x.positive_array, rtol=0, atol=1e-5 * peak)
+        np.testing.assert_allclose(y.negative_array, x.negative_array, rtol=0, atol=1e-5 * peak)
+    # sums in a fixed order: the binned batched run repeats bit for bit
+    c = pkg().run_batched_b200(cfgs, chunk_steps=7, solo_grids=0, deposit="binned", return_fields=True)
+    for x, y in zip(b, c):
+        assert x.ks == y.ks or (x.ks != x.ks and y.ks != y.ks)
+        np.testing.assert_array_equal(x.recombination, y.recombination)
+        np.testing.assert_array_equal(x.positive_array, y.positive_array)

@@ -57,9 +57,9 @@ def test_binding_covers_the_header(lib):
 
 
 def test_host_only_calls_without_a_gpu(lib):
-    assert lib.pic_abi_version() == 7
+    assert lib.pic_abi_version() == 8
     native = __import__("importlib").import_module(pkg().__name__ + "._native")
-    assert native.ABI_VERSION == 7
+    assert native.ABI_VERSION == 8
     assert lib.pic_kernel_launches() == 0  # nothing launched without a GPU
     assert ctypes.sizeof(native.PicGrid) == 200  # 5 int64, 14 double, 11 int32, padded to 8
     assert lib.pic_kpitch(406) == 408
