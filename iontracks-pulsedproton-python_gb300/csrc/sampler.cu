@@ -23,6 +23,11 @@
 // either host architecture.
 #include <stdint.h>
 
+#include <algorithm>
+#include <memory>
+#include <thread>
+#include <vector>
+
 #include "pic_internal.h"
 
 namespace pic {
@@ -64,6 +69,25 @@ struct Pcg64 {
     inline double next_double() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }
 };
 
+// The state `delta` steps on: the LCG's map x -> M x + inc composed with
+// itself delta times, by squaring (F. B. Brown, "Random number generation
+// with arbitrary strides", Trans. Am. Nucl. Soc. 71, 1994): the maps of
+// 1, 2, 4, ... steps are (M^k, inc (M^k - 1) / (M - 1)), doubled as
+// (A, C) -> (A^2, (A + 1) C), and those of delta's set bits applied in turn.
+inline u128 pcg_advance(u128 state, u128 inc, u128 delta) {
+    u128 acc_mult = 1, acc_plus = 0, cur_mult = kPcgMult, cur_plus = inc;
+    while (delta) {
+        if (delta & 1) {
+            acc_mult *= cur_mult;
+            acc_plus = acc_plus * cur_mult + cur_plus;
+        }
+        cur_plus = (cur_mult + 1) * cur_plus;
+        cur_mult *= cur_mult;
+        delta >>= 1;
+    }
+    return acc_mult * state + acc_plus;
+}
+
 }  // namespace
 
 int sample_disc_pcg64(uint64_t *st, double scale, double mid, double radius_sq, int64_t n_wanted, int64_t max_pairs,
@@ -95,13 +119,21 @@ int sample_disc_pcg64(uint64_t *st, double scale, double mid, double radius_sq, 
 // running sum S_k (left to right, as np.cumsum), arrival a_k = (S_k / S_{n-1})
 // * duration (as the in-place divide and multiply), then per bin b the
 // count of a_k in [edges[b], edges[b+1]) -- the last bin closed on the right --
-// which is what np.histogram counts over explicit edges. The stream is drawn
-// twice from the same state, first for S_{n-1}, then to bin each a_k as it is
-// formed (a_k is non-decreasing, so one bin pointer moves forward): no
-// n-element buffer.
-int arrival_counts_pcg64(uint64_t *st, int64_t n, double duration, const double *edges, int64_t n_edges,
-                         int64_t *counts) {
-    const Pcg64 start{((u128)st[0] << 64) | st[1], ((u128)st[2] << 64) | st[3]};
+// which is what np.histogram counts over explicit edges.
+//
+// The running sum is one chain of float64 additions in order (its rounding
+// is the contract); the rest is not. The draws are split over the host's
+// cores, each thread starting from the state advanced to its first draw
+// (pcg_advance); the sum then runs once over them in place; and since a_k
+// never decreases in k, bin b's count is the distance between the first
+// index whose a_k reaches edges[b] and the first reaching edges[b + 1]
+// (binary searches). Small pulses take one sequential pass instead.
+namespace {
+
+constexpr int64_t kArrivalThreadedMin = (int64_t)1 << 20;
+
+void arrival_counts_serial(Pcg64 start, int64_t n, double duration, const double *edges, int64_t n_edges,
+                           int64_t *counts, Pcg64 &end) {
     Pcg64 r = start;
     double last = 0.0;
     for (int64_t k = 0; k < n; ++k) last += r.next_double();
@@ -118,8 +150,58 @@ int arrival_counts_pcg64(uint64_t *st, int64_t n, double duration, const double 
         while (bin < nb - 1 && t >= edges[bin + 1]) ++bin;
         if (bin < nb - 1 || t <= edges[nb]) ++counts[bin];
     }
-    st[0] = (uint64_t)(r.state >> 64);
-    st[1] = (uint64_t)r.state;
+    end = r;
+}
+
+}  // namespace
+
+int arrival_counts_pcg64(uint64_t *st, int64_t n, double duration, const double *edges, int64_t n_edges,
+                         int64_t *counts) {
+    const Pcg64 start{((u128)st[0] << 64) | st[1], ((u128)st[2] << 64) | st[3]};
+    Pcg64 end = start;
+    const int64_t nb = n_edges - 1;
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int64_t threads = std::min<int64_t>(std::max<unsigned>(hw, 1u), 64);
+    if (n < kArrivalThreadedMin || threads < 2) {
+        arrival_counts_serial(start, n, duration, edges, n_edges, counts, end);
+    } else {
+        std::unique_ptr<double[]> S(new double[(size_t)n]);
+        double *u = S.get();
+        std::vector<std::thread> pool;
+        for (int64_t j = 0; j < threads; ++j)
+            pool.emplace_back([=] {
+                const int64_t k0 = n * j / threads, k1 = n * (j + 1) / threads;
+                Pcg64 r{pcg_advance(start.state, start.inc, (u128)k0), start.inc};
+                for (int64_t k = k0; k < k1; ++k) u[k] = r.next_double();
+            });
+        for (auto &t : pool) t.join();
+        double s = 0.0;
+        for (int64_t k = 0; k < n; ++k) {
+            s += u[k];
+            u[k] = s;
+        }
+        const double last = u[n - 1];
+        // first index whose arrival reaches e (strict: passes e)
+        auto first_at = [&](double e, bool strict) {
+            int64_t lo = 0, hi = n;
+            while (lo < hi) {
+                const int64_t mid = lo + (hi - lo) / 2;
+                const double q = u[mid] / last;
+                const double t = q * duration;
+                if (strict ? t > e : t >= e) hi = mid; else lo = mid + 1;
+            }
+            return lo;
+        };
+        int64_t prev = first_at(edges[0], false);
+        for (int64_t b = 0; b < nb; ++b) {
+            const int64_t next = b + 1 < nb ? first_at(edges[b + 1], false) : first_at(edges[nb], true);
+            counts[b] = next > prev ? next - prev : 0;
+            prev = next > prev ? next : prev;
+        }
+        end.state = pcg_advance(start.state, start.inc, (u128)n);
+    }
+    st[0] = (uint64_t)(end.state >> 64);
+    st[1] = (uint64_t)end.state;
     return PIC_OK;
 }
 
