@@ -584,10 +584,10 @@ def run_gb300(args):
                "sample": f"{args.cpu_steps} pulse steps of the same workload after 2 untimed (page first-touch), "
                          f"FP64 oracle, {wall:.1f} s timed"}
 
-    # the benchmark spec's other two ratios, on the same line: the 64-grid sweep
-    # (batched vs the same solves one after another) and the configs' gradient
-    # (full adjoint vs one forward solve), each end to end through the
-    # package's API on this GPU
+    # the benchmark's other two ratios, on the same line: the 64-grid sweep
+    # (batched vs the same solves one after another) and the 10 um column's
+    # gradient (full adjoint vs one forward solve), each end to end through
+    # the package's API on this GPU
     sweep = adjoint = None
     if not args.no_extras:
         if world == 1:
