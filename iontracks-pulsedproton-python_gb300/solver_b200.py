@@ -29,6 +29,7 @@ raises.
 from __future__ import annotations
 
 import copy
+import threading
 from time import perf_counter
 from typing import Optional
 
@@ -108,12 +109,31 @@ def run_simulation_b200(
     last_step = total if max_steps is None else max(0, min(total, int(max_steps)))
     rng = rng if rng is not None else np.random.default_rng(config.seed)
     rng_start = copy.deepcopy(rng.bit_generator.state) if (escalate and dtype == "float32") else None
-    schedule = build_track_schedule(config, rng)
+    # The schedule (one pulse's arrival draws, host cores) on a thread while
+    # the engine allocates and clears its device buffers; the track buffers,
+    # sized by the schedule, come after.
+    drawn = {}
+
+    def draw_schedule():
+        try:
+            drawn["schedule"] = build_track_schedule(config, rng)
+        except BaseException as exc:  # re-raised below
+            drawn["error"] = exc
+
+    worker = threading.Thread(target=draw_schedule, daemon=True)
+    worker.start()
+    try:
+        eng = ChamberEngine(config, dtype=dtype, alpha_cm3_s=alpha_cm3_s, max_tracks=0, shape=shape)
+    finally:
+        worker.join()
+    if "error" in drawn:
+        eng.close()
+        raise drawn["error"]
+    schedule = drawn["schedule"]
     sampler = TrackSampler(rng, config.mid_xy, config.sampling_radius, config.no_xy)
     pulse_steps = int(config.pulse_time_steps)
     max_pulse_tracks = int(schedule[:pulse_steps].sum())
-
-    eng = ChamberEngine(config, dtype=dtype, alpha_cm3_s=alpha_cm3_s, max_tracks=max_pulse_tracks, shape=shape)
+    eng.ensure_track_capacity(max_pulse_tracks)
     torch = eng.torch
     if tune and not shape:
         from .autotune import tune as _tune
