@@ -37,7 +37,8 @@ namespace {
 constexpr int kAdjStreamStages = 4;
 // consumer warps; full electrode, packed, 32-plane items: 12 warps 2.35 ms,
 // 10: 2.42 ms, 15: 2.64 ms; 64-plane items: 12 warps 2.34 ms, 13: 2.60 ms,
-// 14: 2.59 ms
+// 14: 2.59 ms; with the derivative sums by parts: 11 warps 2.232 ms, 12: 2.244
+// ms, 13: 2.451 ms, 14: 2.503 ms
 constexpr int kAdjStreamWarps = 12;
 // Planes per work item: a longer item restarts the ring (two planes of
 // halo) less often -- 64 planes: 2.337 ms per full-electrode step, 32: 2.377
