@@ -19,6 +19,8 @@ from a fixed meta-seed.
 from __future__ import annotations
 
 import copy
+import os
+from concurrent.futures import ThreadPoolExecutor
 import ctypes
 import threading
 import warnings
@@ -374,8 +376,14 @@ def run_batched_b200(
     offsets, samplers = [], []
     track_base = []
     base = 0
-    for c, rng in zip(configs, rngs):
-        sched = build_track_schedule(c, rng)
+    if len(configs) > 1 and len({id(r) for r in rngs}) == len(rngs):
+        # independent generators: the schedules on the host's cores at once
+        # (the native draws release the interpreter)
+        with ThreadPoolExecutor(max_workers=min(len(configs), os.cpu_count() or 1)) as pool:
+            scheds = list(pool.map(build_track_schedule, configs, rngs))
+    else:
+        scheds = [build_track_schedule(c, rng) for c, rng in zip(configs, rngs)]
+    for c, rng, sched in zip(configs, rngs, scheds):
         n_tr = int(sched.sum())
         samplers.append(TrackSampler(rng, c.mid_xy, c.sampling_radius, c.no_xy))
         off = np.zeros(len(sched) + 1, dtype=np.int64)

@@ -63,8 +63,8 @@ def von_neumann_dt(ion_diff, grid_spacing_cm, ion_mobility, Efield_V_cm) -> floa
     mobilities = np.atleast_1d(np.asarray(ion_mobility, dtype=np.float64))
     if diffs.shape != mobilities.shape:
         raise ValueError(
-            f"ion_diff and ion_mobility must describe the same species: got "
-            f"{len(diffs)} diffusion coefficient(s) and {len(mobilities)} mobility/ies."
+            f"{len(diffs)} diffusion coefficients against {len(mobilities)} mobilities: "
+            "ion_diff and ion_mobility need one entry per carrier species each."
         )
     h2 = grid_spacing_cm**2
     dt = 1.0
@@ -135,13 +135,13 @@ class SimulationConfig:
 
         if self.lateral_boundary not in LATERAL_BOUNDARIES:
             raise ValueError(
-                f"lateral_boundary must be one of {LATERAL_BOUNDARIES}, got {self.lateral_boundary!r}."
+                f"unknown lateral_boundary {self.lateral_boundary!r} (known: {', '.join(LATERAL_BOUNDARIES)})."
             )
         if self.scoring_region not in SCORING_REGIONS:
-            raise ValueError(f"scoring_region must be one of {SCORING_REGIONS}, got {self.scoring_region!r}.")
+            raise ValueError(f"unknown scoring_region {self.scoring_region!r} (known: {', '.join(SCORING_REGIONS)}).")
         if isinstance(self.chamber_fill_fraction, bool) or not 0 < self.chamber_fill_fraction <= 1:
             raise ValueError(
-                f"chamber_fill_fraction must be a number in (0, 1], got {self.chamber_fill_fraction!r}."
+                f"chamber_fill_fraction={self.chamber_fill_fraction!r} lies outside (0, 1]."
             )
 
         # grid: rounded, not truncated (config.py:210-212)
@@ -160,9 +160,9 @@ class SimulationConfig:
             )
         if self.no_xy * self.no_xy * self.no_z > self.max_voxels:
             raise ValueError(
-                f"Grid too large: {self.no_xy}x{self.no_xy}x{self.no_z} "
-                f"({self.no_xy * self.no_xy * self.no_z:.3g} voxels). "
-                "Increase grid_size_um or reduce sampled_radius_cm."
+                f"{self.no_xy}x{self.no_xy}x{self.no_z} = {self.no_xy * self.no_xy * self.no_z:.3g} voxels "
+                f"exceeds max_voxels={self.max_voxels:.3g}: use a coarser grid_size_um or a smaller "
+                "sampled_radius_cm."
             )
         # continuous grid centre, a float for odd no_xy too (config.py:254-255)
         self.outer_radius = self.no_xy / 2.0
@@ -170,8 +170,8 @@ class SimulationConfig:
         self.inner_radius = self.outer_radius - self.buffer_radius
         if self.inner_radius <= 0:
             raise ValueError(
-                f"inner_radius = {self.inner_radius:.3g} <= 0 (no_xy={self.no_xy}, "
-                f"buffer_radius={self.buffer_radius}): sampled_radius_cm is too small."
+                f"no sampling region left: inner_radius {self.inner_radius:.3g} is not positive "
+                f"(no_xy {self.no_xy} against buffer_radius {self.buffer_radius})."
             )
         self.inner_radius_sq = self.inner_radius**2
         self.sampling_radius = self.inner_radius * self.chamber_fill_fraction
@@ -191,8 +191,8 @@ class SimulationConfig:
             self.dt = self.von_neumann_dt
         elif self.dt_seconds > self.von_neumann_dt:
             raise ValueError(
-                f"dt_seconds={self.dt_seconds:.4g} s exceeds the von Neumann stability limit of "
-                f"{self.von_neumann_dt:.4g} s for this grid and field."
+                f"unstable time step: dt_seconds {self.dt_seconds:.4g} s is above the von Neumann "
+                f"bound {self.von_neumann_dt:.4g} s of this grid spacing and field."
             )
         else:
             self.dt = float(self.dt_seconds)
@@ -221,8 +221,8 @@ class SimulationConfig:
         )
         if self.n_pulses > 1 and self.pulse_period_steps < self.pulse_time_steps:
             raise ValueError(
-                f"Pulse period is shorter than the pulse itself at this dt "
-                f"({self.pulse_period_steps} < {self.pulse_time_steps} steps)."
+                f"overlapping pulses: a pulse lasts {self.pulse_time_steps} steps but they start "
+                f"every {self.pulse_period_steps} steps at this dt."
             )
         self.total_time_steps = (
             (self.n_pulses - 1) * self.pulse_period_steps + self.pulse_time_steps + self.clearance_time_steps
@@ -240,8 +240,8 @@ class SimulationConfig:
         else:
             if self.track_cutoff_sigmas <= 0:
                 raise ValueError(
-                    f"track_cutoff_sigmas must be positive (or None for no truncation), "
-                    f"got {self.track_cutoff_sigmas!r}."
+                    f"track_cutoff_sigmas={self.track_cutoff_sigmas!r}: give a positive number of "
+                    "sigmas, or None to keep the whole Gaussian."
                 )
             self.track_cutoff_cm = self.track_cutoff_sigmas * self.track_sigma_cm
             self.track_cutoff_voxels = self.track_cutoff_cm / self.unit_length_cm
@@ -291,7 +291,8 @@ class SimulationConfig:
             ("D_negative_cm2_s", self.D_negative),
         ):
             if value <= 0:
-                raise ValueError(f"{name} must be a positive magnitude, got {value!r}.")
+                raise ValueError(f"{name}={value!r}: expected a magnitude above zero (drift directions "
+                                 "follow from the field and the carrier, not from this sign).")
         self.two_carrier_species = not (
             self.mu_positive == self.mu_negative and self.D_positive == self.D_negative
         )

@@ -66,11 +66,11 @@ def test_unknown_energy_without_stopping_power_raises():
         (dict(scoring_region="everywhere"), "scoring_region"),
         (dict(chamber_fill_fraction=0.0), "chamber_fill_fraction"),
         (dict(grid_size_um=100.0, sampled_radius_cm=0.001, buffer_radius=2, no_z_electrode=2), "inner_radius"),
-        (dict(grid_size_um=0.1, sampled_radius_cm=1.0, electrode_gap_cm=1.0), "Grid too large"),
-        (dict(pulse_duration_s=1e-2, repetition_rate_hz=1000.0, n_pulses=2), "Pulse period"),
+        (dict(grid_size_um=0.1, sampled_radius_cm=1.0, electrode_gap_cm=1.0), "exceeds max_voxels"),
+        (dict(pulse_duration_s=1e-2, repetition_rate_hz=1000.0, n_pulses=2), "overlapping pulses"),
         (dict(dt_seconds=1.0), "von Neumann"),
         (dict(track_cutoff_sigmas=-1.0), "track_cutoff_sigmas"),
-        (dict(mu_positive_cm2_Vs=-1.36), "positive magnitude"),
+        (dict(mu_positive_cm2_Vs=-1.36), "magnitude above zero"),
     ],
 )
 def test_degenerate_configs_raise_like_the_reference(kwargs, match):
