@@ -649,7 +649,7 @@ def main():
                     help="skip the sweep and gradient measurements embedded in the default line")
     ap.add_argument("--batched-only", dest="batched_only", action="store_true",
                     help="saturation_sweep: time the batched run only (profiling)")
-    ap.add_argument("--sweep-variant", dest="sweep_variant", choices=["auto", "flat", "stream"], default="auto",
+    ap.add_argument("--sweep-variant", dest="sweep_variant", choices=["auto", "flat", "stream", "mixed"], default="auto",
                     help="saturation_sweep: the batched step kernel (run_batched_b200's variant)")
     ap.add_argument("--sweep-configs", dest="sweep_configs", type=int, default=64,
                     help="saturation_sweep: run the first N of the 64 configurations (profiling-size cases)")

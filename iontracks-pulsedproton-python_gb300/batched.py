@@ -56,11 +56,40 @@ SOLO_MAX_GRIDS = 2
 # three k-vectors each; a grid's tile is as many rows as those fill and a
 # ring stage of any grid stays under STREAM_STAGE_BYTES, so that four stages
 # fit in shared memory; about STREAM_ITEMS_PER_SM items per SM and global
-# step, which the CTAs take from a device-wide queue.
+# step, which the CTAs take from a device-wide queue. Measured over the
+# 64-configuration sweep (device ms of the phases with 60-64 / 40-59 / 20-39
+# active grids): 6 items per SM 190 / 211 / 219, 3 items 179 / 197 / 195,
+# 2 items 177 / 195 / 195, 1 item 176 / 198 / 197; the flat step 200 / 217 /
+# 205. Fewer, longer items pay each item's two priming planes and its tally
+# slot less often.
 STREAM_WARPS = 15
 STREAM_IPT = 3
 STREAM_STAGE_BYTES = 54 * 1024
-STREAM_ITEMS_PER_SM = 6
+STREAM_ITEMS_PER_SM = 2
+# variant="mixed" takes the streaming step on the phases whose active grids
+# hold at least this many interior voxels (fields of ~0.6 GB and more, several
+# times the L2), the flat step on the rest: in the same measurement the flat
+# step was the faster one with 12-19 grids (3.1e7 voxels a step: 27.7 against
+# 28.5 ms) and with 3-11 grids (7.8e6: 128 against 168 ms), where the
+# streaming items are short and the step waits on the slowest CTA. While a
+# float64 re-run runs beside the batch, "mixed" steps flat: the streaming step
+# holds every SM's shared memory, so the re-run's kernels find no room beside
+# it. Even so, end to end on the sweep (which re-runs one configuration in
+# float64) "mixed" took 1.179-1.182 s against 1.165-1.168 s all flat, so
+# "auto" is the flat step; "mixed" pays on sweeps without a re-run (7 % less
+# device time without one).
+STREAM_MIN_VOXELS = 40_000_000
+
+
+def stream_phase(shapes, active, variant: str = "mixed", dtype: str = "float32", persistent: bool = False) -> bool:
+    """Whether a phase of a batched run (grids ``active``, ``shapes[c]`` =
+    (no_xy, nzb, kpitch)) takes the streaming batched step."""
+    if variant == "stream":
+        return True
+    if variant != "mixed" or dtype != "float32" or persistent:
+        return False
+    vox = sum((int(shapes[c][0]) - 2) ** 2 * (int(shapes[c][1]) - 2) for c in active)
+    return vox >= STREAM_MIN_VOXELS
 
 
 def _stage_floats(tj: int, kp: int) -> int:
@@ -327,9 +356,12 @@ def run_batched_b200(
     fused step of the batched launches: "flat" (pic_batched_segment, neighbours
     through L1/L2), "stream" (pic_batched_stream_segment: float32, planes staged
     in a shared-memory ring, items from every grid taken from a device-wide
-    queue), or "auto" (the flat step: over the whole 64-grid sweep the streaming
-    step measured slower, 0.99 against 0.81 s of device time, although its
-    launch in the 64-grid phase alone is the faster, 298 against 331 us).
+    queue), "mixed" (float32: the streaming step on phases whose active grids
+    hold at least STREAM_MIN_VOXELS interior voxels, ``stream_phase``, except
+    while a float64 re-run is in flight; the flat step on the rest, and on
+    float64 and persistent runs), or "auto" (the flat step: end to end on the
+    64-configuration sweep, whose configuration 6 is re-run in float64 beside
+    the batch, it measured 1.165-1.168 s against 1.179-1.182 s "mixed").
     ``escalate``: a float32 configuration whose tallies come back non-finite
     is run again alone with float64 fields from the same generator state
     (run_simulation_b200's ``escalate``), and that Result takes its place.
@@ -350,8 +382,8 @@ def run_batched_b200(
         raise ValueError("chunk_steps must be >= 1")
     if int(solo_grids) < 0:
         raise ValueError("solo_grids must be >= 0")
-    if variant not in ("auto", "flat", "stream"):
-        raise ValueError(f"variant must be 'auto', 'flat' or 'stream', got {variant!r}")
+    if variant not in ("auto", "flat", "stream", "mixed"):
+        raise ValueError(f"variant must be 'auto', 'flat', 'stream' or 'mixed', got {variant!r}")
     if deposit not in ("auto", "binned", "tiles"):
         raise ValueError(f"deposit must be 'auto', 'binned' or 'tiles', got {deposit!r}")
     if variant == "stream" and (dtype != "float32" or persistent):
@@ -473,12 +505,13 @@ def run_batched_b200(
     workspace = torch.zeros(int(wsb.value), dtype=torch.uint8, device=dev)
 
     st = torch.cuda.current_stream(dev).cuda_stream
-    use_stream = variant == "stream"
     stream_tabs = {}  # phase start -> (prepared PicBatchStream, its workspace)
-    if use_stream:
+    if variant in ("stream", "mixed") and dtype == "float32" and not persistent:
         shapes = [(int(g.no_xy), int(g.nzb), int(g.kpitch)) for g in grids]
         for s0, _, tab in phases:
             if solo_grids > 0 and len(tab["active"]) <= solo_grids:
+                continue
+            if not stream_phase(shapes, tab["active"], variant, dtype, persistent):
                 continue
             items_h, tiles_h = _stream_items(shapes, tab["active"], sms)
             sb = ctypes.c_int64()
@@ -626,8 +659,13 @@ def run_batched_b200(
                 L.dep_workspace, L.dep_workspace_bytes = dep_ws.data_ptr(), dep_ws.numel()
                 L.dep_max_tracks, L.dep_total_tiles, L.dep_max_tiles = dep_max_tracks, dep_tiles, dep_max_tiles
                 L.dep_dens_bytes = dep_dens_bytes
+            # "mixed" steps flat while a float64 re-run is in flight: the
+            # streaming step holds every SM's shared memory, the flat one
+            # leaves room for the re-run's kernels beside it
+            streaming = tab["phase_start"] in stream_tabs and not (
+                variant == "mixed" and any(th.is_alive() for th in redo_threads.values()))
             with nvtx_range(f"batched steps ({len(tab['active'])} grids)"):
-                if tab["phase_start"] in stream_tabs:
+                if streaming:
                     bs = stream_tabs[tab["phase_start"]][0]
                     N.check(lib.pic_batched_stream_segment(ctypes.byref(L), ctypes.byref(bs), st),
                             "pic_batched_stream_segment")

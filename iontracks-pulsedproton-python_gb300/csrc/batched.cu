@@ -540,11 +540,9 @@ __global__ void __launch_bounds__(kBinMaxSlots) batched_bin_prep_kernel(
 // Global steps s0 .. s1 - 1 of the launch (at most kBinSteps, their tracks
 // within dep_max_tracks) deposited together. pairs[s - s0]: step s's pairs
 // (a zeroed workspace buffer holding its tracks), or null for a step
-// without tracks. With to_dens, one step into the launch's own dens[bi]
-// instead (the streaming batched step).
+// without tracks.
 template <typename T>
-static int batched_binned_deposit(const BatchLaunch &L, int64_t s0, int64_t s1, const void **pairs, int to_dens,
-                                  cudaStream_t st) {
+static int batched_binned_deposit(const BatchLaunch &L, int64_t s0, int64_t s1, const void **pairs, cudaStream_t st) {
     const BatchedBins<T> B = batched_bins<T>(L);
     BinGroup<T> G{};
     const int64_t t0 = L.step_task_off[s0];
@@ -555,14 +553,10 @@ static int batched_binned_deposit(const BatchLaunch &L, int64_t s0, int64_t s1, 
         G.task_off[q] = L.step_task_off[s] - t0;
         G.track_base[q] = tracks;
         const bool dep = L.step_tracks[s] > 0 && L.step_task_off[s + 1] > L.step_task_off[s];
-        if (to_dens) {
-            G.dens[q] = static_cast<pair_t<T> *>(L.dens[(L.first_step + s) & 1]);
-        } else {
-            G.dens[q] = reinterpret_cast<pair_t<T> *>(B.dens + q * B.dens_stride);
-            if (dep) {
-                cudaError_t e = cudaMemsetAsync(G.dens[q], 0, (size_t)L.dep_dens_bytes, st);
-                if (e != cudaSuccess) return set_cuda_error("cudaMemsetAsync(batched deposition pairs)", e);
-            }
+        G.dens[q] = reinterpret_cast<pair_t<T> *>(B.dens + q * B.dens_stride);
+        if (dep) {
+            cudaError_t e = cudaMemsetAsync(G.dens[q], 0, (size_t)L.dep_dens_bytes, st);
+            if (e != cudaSuccess) return set_cuda_error("cudaMemsetAsync(batched deposition pairs)", e);
         }
         pairs[q] = dep ? G.dens[q] : nullptr;
         tracks += dep ? L.step_tracks[s] : 0;
@@ -590,6 +584,7 @@ int batched_loop_stream(const BatchLaunch &L, const pic_batch_stream *B, cudaStr
         if (rc) return rc;
     }
     auto step_launch = [&](int64_t step, int bi, int bo, const void *dens, void *dens_zero) {
+        if (B) return batched_stream_step(L, *B, bi, bo, step, dens, dens_zero, st);
         if (L.dtype == PIC_F64) {
             if (L.index32) launch_batched_step<double, uint32_t>(L, bi, bo, partials, counters, step, st, dens, dens_zero);
             else launch_batched_step<double, int64_t>(L, bi, bo, partials, counters, step, st, dens, dens_zero);
@@ -599,19 +594,19 @@ int batched_loop_stream(const BatchLaunch &L, const pic_batch_stream *B, cudaStr
         }
         return check_launch("batched_step_kernel");
     };
-    if (L.dep_workspace && !B) {
+    if (L.dep_workspace) {
         // groups of up to kBinSteps global steps (dep_max_tracks tracks):
         // their binned deposition into the workspace's pair buffers, then
-        // their steps, which read those buffers (no pairs to clear: the
-        // launch's own dens buffers stay zero)
+        // their steps (flat or streaming), which read those buffers (no pairs
+        // to clear: the launch's own dens buffers stay zero)
         const void *pairs[kBinSteps];
         for (int64_t s0 = 0; s0 < L.n_steps;) {
             int64_t s1 = s0, tr = 0;
             while (s1 < L.n_steps && s1 - s0 < kBinSteps && tr + L.step_tracks[s1] <= L.dep_max_tracks)
                 tr += L.step_tracks[s1++];
             if (s1 == s0) return set_error(PIC_E_INVALID, "a global step has more tracks than dep_max_tracks");
-            int rc = L.dtype == PIC_F64 ? batched_binned_deposit<double>(L, s0, s1, pairs, 0, st)
-                                        : batched_binned_deposit<float>(L, s0, s1, pairs, 0, st);
+            int rc = L.dtype == PIC_F64 ? batched_binned_deposit<double>(L, s0, s1, pairs, st)
+                                        : batched_binned_deposit<float>(L, s0, s1, pairs, st);
             if (rc) return rc;
             for (int64_t s = s0; s < s1; ++s) {
                 const int64_t step = L.first_step + s;
@@ -628,12 +623,7 @@ int batched_loop_stream(const BatchLaunch &L, const pic_batch_stream *B, cudaStr
         const int bi = (int)(step & 1), bo = bi ^ 1;
         const int64_t t0 = L.step_task_off[s], t1 = L.step_task_off[s + 1];
         const int64_t tracks = L.step_tracks[s];
-        if (tracks > 0 && t1 > t0 && L.dep_workspace) {
-            const void *pairs[1];
-            int rc = L.dtype == PIC_F64 ? batched_binned_deposit<double>(L, s, s + 1, pairs, 1, st)
-                                        : batched_binned_deposit<float>(L, s, s + 1, pairs, 1, st);
-            if (rc) return rc;
-        } else if (tracks > 0 && t1 > t0) {
+        if (tracks > 0 && t1 > t0) {
             const unsigned blocks = (unsigned)L.step_blocks[s];
             if (L.dtype == PIC_F64)
                 batched_deposit_kernel<double><<<blocks, kDepThreads, 0, st>>>(
@@ -645,11 +635,6 @@ int batched_loop_stream(const BatchLaunch &L, const pic_batch_stream *B, cudaStr
                     L.ys, (float2 *)L.dens[bi], L.counts);
             int rc = check_launch("batched_deposit_kernel");
             if (rc) return rc;
-        }
-        if (B) {
-            int rc = batched_stream_step(L, *B, bi, bo, step, st);
-            if (rc) return rc;
-            continue;
         }
         int rc = step_launch(step, bi, bo, L.dens[bi], L.dens[bo]);
         if (rc) return rc;

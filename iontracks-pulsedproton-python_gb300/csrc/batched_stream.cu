@@ -382,7 +382,7 @@ int batched_stream_prepare(const pic_batch_cfg *cfgs, int32_t n_cfgs, const int3
 }
 
 int batched_stream_step(const BatchLaunch &L, const pic_batch_stream &B, int bi, int bo, int64_t step,
-                        cudaStream_t st) {
+                        const void *dens, void *dens_zero, cudaStream_t st) {
     char *base = static_cast<char *>(B.workspace);
     BsArgs b;
     b.grids = reinterpret_cast<const BsGrid *>(base + off_grids(B.n_cfgs));
@@ -392,8 +392,8 @@ int batched_stream_step(const BatchLaunch &L, const pic_batch_stream &B, int bi,
     b.neg_in = (const float *)L.neg[bi];
     b.pos_out = (float *)L.pos[bo];
     b.neg_out = (float *)L.neg[bo];
-    b.dens = (const float2 *)L.dens[bi];
-    b.dens_zero = (float2 *)L.dens[bo];
+    b.dens = (const float2 *)dens;
+    b.dens_zero = (float2 *)dens_zero;
     b.tally = L.tally;
     b.step = step;
     b.hdr = reinterpret_cast<BsHeader *>(base);

@@ -223,7 +223,9 @@ int launch_deposit_steps(const pic_grid *g, const double *xs, const double *ys, 
                          cudaStream_t st);
 // Kernel launches issued by this library so far (every launch site reports
 // to check_launch; a captured graph's launches count at each replay).
-void count_launches(int64_t n);using BatchLaunch = pic_batch_launch;
+void count_launches(int64_t n);
+
+using BatchLaunch = pic_batch_launch;
 int batched_workspace_bytes(int32_t n_blocks, int32_t n_cfgs, int64_t *bytes);
 int batched_loop(const BatchLaunch &L, cudaStream_t st);
 int batched_persistent(const BatchLaunch &L, const int64_t *step_task_off, const int64_t *step_tracks,
@@ -234,8 +236,10 @@ int batched_stream_workspace_bytes(int32_t n_cfgs, int32_t n_items, int32_t cons
 int batched_stream_prepare(const pic_batch_cfg *cfgs, int32_t n_cfgs, const int32_t *items, int32_t n_items,
                            const int32_t *tile_rows, int32_t consumer_warps, void *ws, int64_t ws_bytes,
                            cudaStream_t st, pic_batch_stream *out);
+// dens: the step's deposition pairs in the packed layout; dens_zero: pairs the
+// step clears for the next one (null: none)
 int batched_stream_step(const BatchLaunch &L, const pic_batch_stream &B, int bi, int bo, int64_t step,
-                        cudaStream_t st);
+                        const void *dens, void *dens_zero, cudaStream_t st);
 int batched_stream_status(const pic_batch_stream &B, int32_t reset, cudaStream_t st, int32_t *status);
 // batched_loop with B non-null runs the streaming step instead of the flat one.
 int batched_loop_stream(const BatchLaunch &L, const pic_batch_stream *B, cudaStream_t st);

@@ -263,7 +263,7 @@ def test_stream_items_cover_every_interior_voxel_once():
     """The streaming batched step's item table (CPU): for every phase of the
     64-grid sweep, each active grid's interior rows x planes are covered
     exactly once, a grid's items are consecutive, tiles fit the consumer
-    threads and a ring stage, and about six items per SM come out."""
+    threads and a ring stage, and every SM gets an item of the heavy phase."""
     B = _stream_mod()
     cfgs = pkg().saturation_sweep_configs()
     shapes = [(int(c.no_xy), int(c.no_z_with_buffer), (int(c.no_z_with_buffer) + 7) // 8 * 8) for c in cfgs]
@@ -289,9 +289,32 @@ def test_stream_items_cover_every_interior_voxel_once():
                     cover[i0:i1, j0:min(j0 + tj, n - 1)] += 1
                 assert (cover[1:-1, 1:-1] == 1).all() and cover[0].sum() == 0 and cover[-1].sum() == 0
                 assert cover[:, 0].sum() == 0 and cover[:, -1].sum() == 0
-        # the heavy first phase: a few items per SM
+        # the heavy first phase: about STREAM_ITEMS_PER_SM items per SM
         items, _ = B._stream_items(shapes, list(range(64)), sms)
-        assert len(items) >= 2 * sms
+        assert len(items) >= sms
+
+
+def test_mixed_takes_the_streaming_step_on_the_heavy_phases_only():
+    """variant="mixed" (CPU): the sweep's phases of many grids (above
+    STREAM_MIN_VOXELS interior voxels a step) take the streaming step, those
+    of a few grids the flat one; float64, persistent, variant="flat" and
+    variant="auto" runs never stream, variant="stream" always does."""
+    B = _stream_mod()
+    cfgs = pkg().saturation_sweep_configs()
+    shapes = [(int(c.no_xy), int(c.no_z_with_buffer), (int(c.no_z_with_buffer) + 7) // 8 * 8) for c in cfgs]
+    totals = [int(c.total_time_steps) for c in cfgs]
+    picks = [(len(a), B.stream_phase(shapes, a)) for _, _, a in B._phases(totals)]
+    assert picks[0] == (64, True)
+    assert all(not st for n, st in picks if n <= 19) and all(st for n, st in picks if n >= 40)
+    # the choice only ever goes from streaming to flat: phases lose grids
+    flags = [st for _, st in picks]
+    assert flags == sorted(flags, reverse=True)
+    every = list(range(64))
+    assert not B.stream_phase(shapes, every, "flat")
+    assert not B.stream_phase(shapes, every, "auto")
+    assert not B.stream_phase(shapes, every, "mixed", dtype="float64")
+    assert not B.stream_phase(shapes, every, "mixed", persistent=True)
+    assert B.stream_phase(shapes, [63], "stream")
 
 
 def test_stream_variant_arguments_are_checked_before_device_work():
@@ -321,6 +344,33 @@ def test_stream_batched_step_matches_the_flat_one(solo):
         np.testing.assert_allclose(y.recombination, x.recombination, rtol=0,
                                    atol=1e-5 * max(np.abs(x.recombination).max(), 1e-300))
         np.testing.assert_allclose(y.injected_positive, x.injected_positive, rtol=1e-5, atol=0)
+        peak = max(np.abs(x.positive_array).max(), 1e-300)
+        np.testing.assert_allclose(y.positive_array, x.positive_array, rtol=0, atol=1e-5 * peak)
+        np.testing.assert_allclose(y.negative_array, x.negative_array, rtol=0, atol=1e-5 * peak)
+
+
+@pytest.mark.gpu
+def test_mixed_switches_from_the_streaming_to_the_flat_step(monkeypatch):
+    """variant="mixed" with the streaming threshold set between the mixed
+    batch's phases: the first phases stream, the later ones run flat (and the
+    last ones solo), handing the fields, pairs and tallies across; against an
+    all-flat run: identical tracks, k_s and tallies within 1e-5, fields within
+    1e-5 of their peak."""
+    B = _stream_mod()
+    cfgs = _mixed_batch()
+    shapes = [(int(c.no_xy), int(c.no_z_with_buffer), (int(c.no_z_with_buffer) + 7) // 8 * 8) for c in cfgs]
+    phases = B._phases([int(c.total_time_steps) for c in cfgs])
+    vox = [sum((shapes[c][0] - 2) ** 2 * (shapes[c][1] - 2) for c in a) for _, _, a in phases]
+    assert len(vox) >= 3 and vox[0] > vox[1]
+    monkeypatch.setattr(B, "STREAM_MIN_VOXELS", vox[1])
+    assert [B.stream_phase(shapes, a) for _, _, a in phases][:3] == [True, True, False]
+    a = pkg().run_batched_b200(cfgs, chunk_steps=7, variant="flat", return_fields=True)
+    b = pkg().run_batched_b200(cfgs, chunk_steps=7, variant="mixed", return_fields=True)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x.track_density_xy, y.track_density_xy)
+        assert abs(x.ks - y.ks) <= KS_ABS
+        np.testing.assert_allclose(y.recombination, x.recombination, rtol=0,
+                                   atol=1e-5 * max(np.abs(x.recombination).max(), 1e-300))
         peak = max(np.abs(x.positive_array).max(), 1e-300)
         np.testing.assert_allclose(y.positive_array, x.positive_array, rtol=0, atol=1e-5 * peak)
         np.testing.assert_allclose(y.negative_array, x.negative_array, rtol=0, atol=1e-5 * peak)
