@@ -38,8 +38,11 @@ constexpr int kAdjStreamStages = 4;
 // consumer warps; full electrode, packed, 32-plane items: 12 warps 2.35 ms,
 // 10: 2.42 ms, 15: 2.64 ms; 64-plane items: 12 warps 2.34 ms, 13: 2.60 ms,
 // 14: 2.59 ms; with the derivative sums by parts: 11 warps 2.232 ms, 12: 2.244
-// ms, 13: 2.451 ms, 14: 2.503 ms
-constexpr int kAdjStreamWarps = 12;
+// ms, 13: 2.451 ms, 14: 2.503 ms; with each slot's values formed once per
+// item: 11 warps 2.146 ms, 10: 2.160 ms. Twelve warps in all (eleven and the
+// producer) leave each SM sub-partition three warps and so 168 registers a
+// thread; thirteen would cap it at 128.
+constexpr int kAdjStreamWarps = 11;
 // Planes per work item: a longer item restarts the ring (two planes of
 // halo) less often -- 64 planes: 2.337 ms per full-electrode step, 32: 2.377
 // ms, 96: 2.341 ms, 128: 2.434 ms; on 608 x 608 x 406 (6.6 items of 64
@@ -48,6 +51,10 @@ constexpr int kAdjStreamWarps = 12;
 // kAdjStreamMinItems.
 constexpr int kAdjStreamPlanes = 64, kAdjStreamPlanesShort = 32, kAdjStreamMinItems = 6;
 constexpr int kAdjStreamMaxIpt = 4;
+// flags of a consumer slot (bits 0-3: in the gap, 4-7: valid k, 16-23: the
+// index of its deposition pair in a stage)
+constexpr uint32_t kSlotJm = 1u << 8, kSlotJp = 1u << 9, kSlotKm = 1u << 10, kSlotKp = 1u << 11,
+                   kSlotRingJ = 1u << 12, kSlotLive = 1u << 13;
 constexpr int kAdjStreamSmemMax = 220 * 1024;
 
 struct AdjStreamArgs {
@@ -176,6 +183,39 @@ __global__ void __launch_bounds__((kAdjStreamWarps + 1) * 32, 1) adjoint_stream_
             const int nplanes = ci_hi - ci_lo + 2;
             const int n_all = (cj_hi - cj_lo) * c4;
             const int dq = (cj_lo - 1) & 3;  // pair of staged row q: dq + q
+            // per slot, fixed over the item's planes: its offset in a stage
+            // (staged row rs, k0: rs kp + k0; its output offset within a plane
+            // is that plus (cj_lo - 1) kp), dy^2 of the scored test, and flags
+            // (k gap / valid bits, lateral and k neighbours present, ring
+            // rows, the pair index dq + rs). Formed once per item instead of
+            // once per plane: 2.146 against 2.233 ms a full-electrode step.
+            int so_[IPT];
+            uint32_t dy2_[IPT], fl_[IPT];
+            const int64_t oo_base = (int64_t)(cj_lo - 1) * kp;
+#pragma unroll
+            for (int kk = 0; kk < IPT; ++kk) {
+                const int sl = ctid + kk * nct;
+                const bool live = sl < n_all;
+                const int r = live ? sl / c4 : 0, c = live ? sl - r * c4 : 0;
+                const int rs = r + 1;  // staged row of this column
+                const int cj = cj_lo + r;
+                const int k0 = 4 * c;
+                so_[kk] = rs * kp + k0;
+                const int dy = 2 * cj - a.two_mid;
+                dy2_[kk] = (uint32_t)(dy * dy);
+                uint32_t f = live ? kSlotLive : 0u;
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    if (k0 + e >= a.nze && k0 + e < a.gap_end) f |= 1u << e;
+                    if (k0 + e >= 1 && k0 + e <= a.nzb - 2) f |= 16u << e;
+                }
+                if (cj - 1 >= 1) f |= kSlotJm;
+                if (cj + 1 <= n - 2) f |= kSlotJp;
+                if (k0 >= 1) f |= kSlotKm;
+                if (k0 + 4 < kp) f |= kSlotKp;
+                if (cj == 1 || cj == n - 2) f |= kSlotRingJ;
+                fl_[kk] = f | ((uint32_t)(dq + rs) << 16);
+            }
             int sm_ = (int)(g % S), sc_ = sm_ + 1 == S ? 0 : sm_ + 1, sp_ = sc_ + 1 == S ? 0 : sc_ + 1;
             uint32_t pm_ = (uint32_t)((g / S) & 1), pc_ = sc_ == 0 ? pm_ ^ 1u : pm_, pp_ = sp_ == 0 ? pc_ ^ 1u : pc_;
             if (!mbar_wait(&full[sm_], pm_, a.status, 13) || !mbar_wait(&full[sc_], pc_, a.status, 13)) abort_flag = 1;
@@ -194,33 +234,30 @@ __global__ void __launch_bounds__((kAdjStreamWarps + 1) * 32, 1) adjoint_stream_
                 float2 G0 = make_float2(0.f, 0.f), G1 = G0, G2 = G0, G3 = G0, G4 = G0;
 #pragma unroll
                 for (int kk = 0; kk < IPT; ++kk) {
-                    const int sl = ctid + kk * nct;
-                    if (sl >= n_all) break;
-                    const int r = sl / c4, c = sl - r * c4;
-                    const int rs = r + 1;  // staged row of this column
-                    const int cj = cj_lo + r;
-                    const int k0 = 4 * c;
-                    const int o = rs * kp + k0;
+                    const uint32_t fl = fl_[kk];
+                    if (!(fl & kSlotLive)) break;
+                    const int o = so_[kk];
                     bool g4[4], valid[4], sc[4];
-                    const int dy = 2 * cj - a.two_mid;
-                    const bool scored = dx2 + (uint32_t)(dy * dy) <= a.thr4;
+                    const bool scored = dx2 + dy2_[kk] <= a.thr4;
 #pragma unroll
                     for (int e = 0; e < 4; ++e) {
-                        g4[e] = (k0 + e >= a.nze) && (k0 + e < a.gap_end);
-                        valid[e] = (k0 + e >= 1) && (k0 + e <= a.nzb - 2);
+                        g4[e] = (fl >> e) & 1u;
+                        valid[e] = (fl >> (4 + e)) & 1u;
                         sc[e] = scored && g4[e];
                     }
-                    const float2 dpr = has_dens ? reinterpret_cast<const float2 *>(Sc + dens_off)[dq + rs]
+                    const float2 dpr = has_dens ? reinterpret_cast<const float2 *>(Sc + dens_off)[fl >> 16]
                                                 : make_float2(0.f, 0.f);
                     const float dc = dpr.x, dl = dpr.y;  // this column's deposition, its neighbours' sum
-                    const bool jm_in = cj - 1 >= 1, jp_in = cj + 1 <= n - 2;
+                    const bool jm_in = fl & kSlotJm, jp_in = fl & kSlotJp;
 
                     // mu = lambda_{s+1}: zero on the end planes and the padding as
                     // every adjoint step writes it; zero on ring columns by the
-                    // interior tests of the neighbours
+                    // interior tests of the neighbours. (Carrying planes ci - 1
+                    // and ci over from the previous plane in registers instead
+                    // measured slower: 2.26-2.32 against 2.16 ms, it spills.)
                     const float4 MP = lds4(Sc + o), MN = lds4(Sc + spec + o);
-                    const float mp_km = k0 >= 1 ? Sc[o - 1] : 0.f, mn_km = k0 >= 1 ? Sc[spec + o - 1] : 0.f;
-                    const float mp_kp = k0 + 4 < kp ? Sc[o + 4] : 0.f, mn_kp = k0 + 4 < kp ? Sc[spec + o + 4] : 0.f;
+                    const float mp_km = (fl & kSlotKm) ? Sc[o - 1] : 0.f, mn_km = (fl & kSlotKm) ? Sc[spec + o - 1] : 0.f;
+                    const float mp_kp = (fl & kSlotKp) ? Sc[o + 4] : 0.f, mn_kp = (fl & kSlotKp) ? Sc[spec + o + 4] : 0.f;
                     const float4 Z = make_float4(0.f, 0.f, 0.f, 0.f);
                     const float4 A0 = im_in ? lds4(Sm + o) : Z, B0 = im_in ? lds4(Sm + spec + o) : Z;
                     const float4 A1 = ip_in ? lds4(Sp + o) : Z, B1 = ip_in ? lds4(Sp + spec + o) : Z;
@@ -265,15 +302,19 @@ __global__ void __launch_bounds__((kAdjStreamWarps + 1) * 32, 1) adjoint_stream_
                                                   valid[2] ? lph.x : 0.f, valid[3] ? lph.y : 0.f);
                     const float4 ON = make_float4(valid[0] ? lnl.x : 0.f, valid[1] ? lnl.y : 0.f,
                                                   valid[2] ? lnh.x : 0.f, valid[3] ? lnh.y : 0.f);
-                    const int64_t col = (int64_t)ci * n + cj;
-                    st4(a.lp_out + col * kp + k0, OP);
-                    st4(a.ln_out + col * kp + k0, ON);
+                    const int64_t out = (int64_t)ci * n * kp + oo_base + o;
+                    st4(a.lp_out + out, OP);
+                    st4(a.ln_out + out, ON);
 
                     // ring columns next to this interior column: (ri, cj),
                     // (ci, rj) get lat * mu + carry; the corner (ri, rj) the carry
                     // (mu and the carry are zero on the end planes and padding)
-                    const bool lo_i = ci == 1, hi_i = ci == n - 2, lo_j = cj == 1, hi_j = cj == n - 2;
-                    if (lo_i || hi_i || lo_j || hi_j) {
+                    const bool lo_i = ci == 1, hi_i = ci == n - 2;
+                    if (lo_i || hi_i || (fl & kSlotRingJ)) {
+                        const int rs = (int)(fl >> 16) - dq;  // staged row of this column
+                        const int cj = cj_lo - 1 + rs;
+                        const int k0 = o - rs * kp;
+                        const bool lo_j = cj == 1, hi_j = cj == n - 2;
                         for (int tgt = 0; tgt < 3; ++tgt) {
                             int ri = ci, rj = cj, row = rs;
                             const float *Sr = Sc;
