@@ -234,7 +234,7 @@ def _max_abs_diff(a, b):
     return worst
 
 
-def sweep_measure(n_configs=64, batched_only=False, rank=0, world=1, variant="auto"):
+def sweep_measure(n_configs=64, batched_only=False, rank=0, world=1, variant="auto", warmup=3):
     """The 64-configuration saturation sweep: one batched run against the same
     configurations solved one after another with the plain solver on the
     same GPU, both end to end (host track sampling, uploads, all steps,
@@ -246,9 +246,11 @@ def sweep_measure(n_configs=64, batched_only=False, rank=0, world=1, variant="au
     idx = list(range(len(every)))[rank::world]  # the sweep's configurations shared out over the GPUs
     cfgs = [every[i] for i in idx]
     vox = sum(_interior(c) * int(c.total_time_steps) for c in cfgs)
-    # warm-up: load the kernels, pay first-use costs outside the timing
-    pkg.run_batched_b200(cfgs[:2], variant=variant)
-    pkg.run_simulation_b200(cfgs[0], progress=False, return_fields=False)
+    # warm-up (``warmup`` rounds): load the kernels, pay first-use costs
+    # outside the timing
+    for _ in range(max(1, warmup)):
+        pkg.run_batched_b200(cfgs[:2], variant=variant)
+        pkg.run_simulation_b200(cfgs[0], progress=False, return_fields=False)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     batch = pkg.run_batched_b200(cfgs, variant=variant)
@@ -281,7 +283,7 @@ def run_sweep(args):
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
     replicas = importlib.import_module(PACKAGE + ".replicas")
-    m = sweep_measure(args.sweep_configs, args.batched_only, rank, world, args.sweep_variant)
+    m = sweep_measure(args.sweep_configs, args.batched_only, rank, world, args.sweep_variant, args.warmup)
     value = replicas.whole_job_rate(m["interior_voxel_steps"], m["batched_s"])
     t_batch = replicas.max_over_ranks(m["batched_s"])
     vox = replicas.sum_over_ranks(m["interior_voxel_steps"])
@@ -299,9 +301,10 @@ def run_sweep(args):
             "metric": "interior voxel-steps/s, 64-config saturation sweep", "value": value,
             "unit": "voxel-steps/s", "n_gpus": world, "steps": int(max(c.total_time_steps for c in
                                                                         _pkg().saturation_sweep_configs())),
-            "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic",
-            "config": {"workload": SWEEP_DESC.format(n=m["n_total"]), "interior_voxel_steps": vox},
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "strong",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": SWEEP_DESC.format(n=m["n_total"]), "interior_voxel_steps": vox,
+                       "warmup_unit": "a two-configuration batched run and one plain solve"},
             "batched_s": t_batch, "sequential_plain_s": t_plain,
             "speedup_vs_sequential": None if t_plain is None else t_plain / t_batch,
             "max_abs_dks_batched_vs_plain": dks, "max_abs_dks_batched_vs_fp64_oracle": dko,
@@ -445,7 +448,7 @@ def run_full_electrode_run(args):
     total = int(cfg.total_time_steps)
     pulse = int(cfg.pulse_time_steps) * int(cfg.n_pulses)
     steps = total if args.run_steps <= 0 else min(total, int(args.run_steps))
-    # warm-up: load the library, resolve the launch shape
+    # warm-up: load the library, resolve the launch shape (8 steps)
     pkg.run_simulation_b200(cfg, progress=False, return_fields=False, max_steps=8)
     torch.cuda.synchronize()
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
@@ -458,7 +461,7 @@ def run_full_electrode_run(args):
     if rank == 0:
         print(json.dumps({
             "metric": "interior voxel-steps/s, whole 10-pulse run", "value": vox * steps / wall,
-            "unit": "voxel-steps/s", "n_gpus": world, "steps": steps, "warmup": 1,
+            "unit": "voxel-steps/s", "n_gpus": world, "steps": steps, "warmup": 8,
             "ms_per_step": 1e3 * wall / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
             "config": _workload_config(cfg, desc + "; the whole run", 0, world),
