@@ -38,11 +38,17 @@ from .state import Diagnostics, collection_efficiency
 
 # The batched step runs 4 resident 256-thread blocks per SM (float32, 64
 # registers).
-# Items per block are chosen per phase for about four blocks per resident slot:
-# few, long blocks amortise each block's set-up and reduction on the big
-# phases; enough blocks keep every SM busy when few small grids remain.
+# Items per block are chosen per phase for about WAVES blocks per resident
+# slot on phases of at least SMALL_PHASE_ITEMS items, one block per slot
+# below: few, long blocks amortise each block's set-up and reduction. Measured
+# over the 64-configuration sweep (device ms of the phases with 60-64 / 40-59
+# / 20-39 / 12-19 / 3-11 active grids), blocks per slot 1: 229 / 264 / 251 /
+# 27.0 / 110; 2: 206 / 234 / 210 / 26.5 / 116; 4: 199 / 216 / 204 / 27.5 /
+# 127; 8: 197 / 218 / 211 / 28.8 / 146; 16: 205 / 230 / 228 / 32 / 185.
 BLOCKS_PER_SM = 4
 WAVES = 4
+WAVES_SMALL = 1
+SMALL_PHASE_ITEMS = 10_000_000  # four-vector items a step (4e7 voxels)
 MIN_ITEMS_PER_BLOCK = 256
 MAX_ITEMS_PER_BLOCK = 1 << 16
 # Phases with at most this many active grids step each grid alone with the
@@ -147,7 +153,8 @@ class PicBatchStream(ctypes.Structure):
 
 def items_per_block(total_items: int, sms: int) -> int:
     """Work items per block for a phase of ``total_items`` items."""
-    want = -(-int(total_items) // (WAVES * BLOCKS_PER_SM * max(1, sms)))
+    waves = WAVES if int(total_items) >= SMALL_PHASE_ITEMS else WAVES_SMALL
+    want = -(-int(total_items) // (waves * BLOCKS_PER_SM * max(1, sms)))
     want = -(-want // 256) * 256
     return max(MIN_ITEMS_PER_BLOCK, min(MAX_ITEMS_PER_BLOCK, want))
 

@@ -294,6 +294,21 @@ def test_stream_items_cover_every_interior_voxel_once():
         assert len(items) >= sms
 
 
+def test_items_per_block_takes_one_block_per_slot_on_small_phases():
+    """The flat batched step's work split (CPU): about WAVES blocks per
+    resident slot on phases of at least SMALL_PHASE_ITEMS items, one below,
+    in multiples of 256 items, within the bounds."""
+    B = _stream_mod()
+    slots = B.BLOCKS_PER_SM * 152
+    big, small = B.SMALL_PHASE_ITEMS * 2, B.SMALL_PHASE_ITEMS // 5
+    ipb_big, ipb_small = B.items_per_block(big, 152), B.items_per_block(small, 152)
+    assert ipb_big % 256 == 0 and ipb_small % 256 == 0
+    assert -(-big // ipb_big) <= B.WAVES * slots < -(-big // ipb_big) + slots
+    assert -(-small // ipb_small) <= B.WAVES_SMALL * slots
+    assert B.items_per_block(1, 152) == B.MIN_ITEMS_PER_BLOCK
+    assert B.items_per_block(1 << 40, 1) == B.MAX_ITEMS_PER_BLOCK
+
+
 def test_mixed_takes_the_streaming_step_on_the_heavy_phases_only():
     """variant="mixed" (CPU): the sweep's phases of many grids (above
     STREAM_MIN_VOXELS interior voxels a step) take the streaming step, those
