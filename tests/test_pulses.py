@@ -176,3 +176,23 @@ def test_threaded_arrival_counts_equal_numpys_at_full_electrode_size(seed):
     np.testing.assert_array_equal(got, want)
     assert r_native.bit_generator.state == r_numpy.bit_generator.state
     np.testing.assert_array_equal(r_native.random(8), r_numpy.random(8))
+
+
+def test_schedules_drawn_on_threads_equal_the_sequential_ones():
+    """The batched driver draws its configurations' schedules on a thread
+    pool (each with its own generator; the native draws release the
+    interpreter): the 64 sweep schedules and the generators' end states equal
+    those of one-after-another draws."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    P = pkg()
+    pulses = importlib.import_module(P.__name__ + ".pulses")
+    cfgs = P.saturation_sweep_configs()
+    seq_rngs = [np.random.default_rng(c.seed) for c in cfgs]
+    par_rngs = [np.random.default_rng(c.seed) for c in cfgs]
+    seq = [pulses.build_track_schedule(c, r) for c, r in zip(cfgs, seq_rngs)]
+    with ThreadPoolExecutor(max_workers=8) as pool:
+        par = list(pool.map(pulses.build_track_schedule, cfgs, par_rngs))
+    for a, b, ra, rb in zip(seq, par, seq_rngs, par_rngs):
+        np.testing.assert_array_equal(a, b)
+        assert ra.bit_generator.state == rb.bit_generator.state
