@@ -564,7 +564,9 @@ int pic_batched_status(const pic_batch_launch *launch, uintptr_t stream, int32_t
  * whenever the item table changes (a grid finished).
  * pic_batched_stream_segment runs global steps [first_step, first_step +
  * n_steps) of `launch` (its task tables and buffers; its flat work table and
- * workspace are not used) with the prepared tables.
+ * workspace are not used) with the prepared tables. The deposition is the
+ * one pic_batched_segment runs: binned, up to 8 global steps per launch pair,
+ * when launch->dep_workspace is set, else the tile form.
  * pic_batched_stream_status reads the workspace's status word: 0, 1-3 when a
  * bounded wait of the copy ring ran out, 7 when an item was refused on the
  * device; with reset != 0 a non-zero word is cleared together with the queue
