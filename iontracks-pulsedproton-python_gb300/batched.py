@@ -313,6 +313,32 @@ def _task_tables(offsets, totals, track_base, no_xy=None):
     return step_task_off, step_tracks, c_idx.astype(np.int32), F[s_idx, c_idx], t_prefix, step_blocks
 
 
+# The first chunk of global steps is sampled on the host before the device
+# has anything to run; later chunks are sampled while the device runs the one
+# before. Chunks start at FIRST_CHUNK_STEPS steps and double up to
+# chunk_steps, so the device starts after a small first chunk (the sweep's
+# all-grid phase draws ~31 000 tracks a step: 268 steps of them were ~50 ms
+# of host sampling ahead of the first launch).
+FIRST_CHUNK_STEPS = 16
+
+
+def _ramp_chunks(phases, chunk_steps: int, first: int = FIRST_CHUNK_STEPS):
+    """Chunks (c0, c1, phase table + phase_start) of the ``phases`` of a
+    batched run: every global step once, in order, no chunk across a phase
+    boundary, sizes from ``min(first, chunk_steps)`` doubling up to
+    ``chunk_steps`` over the run."""
+    out = []
+    size = max(1, min(int(first), int(chunk_steps)))
+    for s0, s1, tab in phases:
+        c0 = s0
+        while c0 < s1:
+            c1 = min(c0 + size, s1)
+            out.append((c0, c1, dict(tab, phase_start=s0)))
+            c0 = c1
+            size = min(2 * size, int(chunk_steps))
+    return out
+
+
 def _work_table(items, active, sms: int) -> dict:
     """Blocks of one batched launch over the ``active`` grids (``items[c]`` =
     grid c's work items): each grid gets contiguous blocks, and block b of a
@@ -352,7 +378,10 @@ def run_batched_b200(
 
     Equivalent to ``[run_simulation_b200(c) for c in configs]`` (same tracks,
     same tallies to float32 rounding) but with all grids advanced together.
-    ``persistent`` runs each chunk of ``chunk_steps`` global steps as one
+    The global steps run in chunks of up to ``chunk_steps`` (the first
+    chunks shorter: FIRST_CHUNK_STEPS doubling, ``_ramp_chunks``), each
+    sampled on the host while the device runs the one before.
+    ``persistent`` runs each chunk as one
     persistent launch (``pic_batched_persistent``: deposition and step phases
     separated by device-wide barriers); otherwise (the default) each global
     step is two launches (``pic_batched_segment``). Measured on GB300 over the
@@ -562,10 +591,9 @@ def run_batched_b200(
 
     sto_dev = torch.from_numpy(step_task_off).to(dev)
     stt_dev = torch.from_numpy(np.ascontiguousarray(step_tracks, dtype=np.int64)).to(dev)
-    # chunks of global steps; chunk (c0, c1) needs grid c's tracks
-    # [offsets[c][min(c0, T_c)], offsets[c][min(c1, T_c)])
-    chunks = [(c0, min(c0 + chunk_steps, s1), dict(tab, phase_start=s0)) for s0, s1, tab in phases
-              for c0 in range(s0, s1, chunk_steps)]
+    # chunks of global steps (a ramp from FIRST_CHUNK_STEPS); chunk (c0, c1)
+    # needs grid c's tracks [offsets[c][min(c0, T_c)], offsets[c][min(c1, T_c)])
+    chunks = _ramp_chunks(phases, int(chunk_steps))
 
     def jobs_of(c0, c1):
         out = []

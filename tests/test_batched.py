@@ -83,6 +83,30 @@ def test_deposition_tasks_of_every_global_step():
             assert blocks[s] == sum(tiles(sizes[c]) * min(32, max(1, -(-m // 32))) for c, _, m in want)
 
 
+def test_chunks_ramp_up_and_cover_every_step_once():
+    """The batched driver's chunks (CPU): every global step once, in order,
+    none across a phase boundary, the first FIRST_CHUNK_STEPS long (or
+    chunk_steps if shorter), then doubling up to chunk_steps."""
+    b = _stream_mod()
+    cfgs = pkg().saturation_sweep_configs()
+    phases = b._phases([int(c.total_time_steps) for c in cfgs])
+    tabs = [(s0, s1, {"active": a}) for s0, s1, a in phases]
+    for chunk_steps in (1, 7, 16, 100, 512):
+        chunks = b._ramp_chunks(tabs, chunk_steps)
+        assert chunks[0][0] == 0 and chunks[-1][1] == phases[-1][1]
+        assert all(x[1] == y[0] for x, y in zip(chunks, chunks[1:]))
+        starts = {s0: s1 for s0, s1, _ in phases}
+        for c0, c1, tab in chunks:
+            s0 = tab["phase_start"]
+            assert s0 <= c0 < c1 <= starts[s0] and 1 <= c1 - c0 <= chunk_steps
+        assert chunks[0][1] - chunks[0][0] == min(b.FIRST_CHUNK_STEPS, chunk_steps, phases[0][1])
+        # sizes double until chunk_steps, except where a phase ends first
+        size = min(b.FIRST_CHUNK_STEPS, chunk_steps)
+        for c0, c1, tab in chunks:
+            assert c1 - c0 == min(size, starts[tab["phase_start"]] - c0)
+            size = min(2 * size, chunk_steps)
+
+
 def test_work_tables_cover_each_active_grid_once():
     """One batched launch's blocks: every active grid's items split into
     contiguous, non-overlapping block ranges covering them exactly; inactive
