@@ -318,21 +318,33 @@ def _task_tables(offsets, totals, track_base, no_xy=None):
 # before. Chunks start at FIRST_CHUNK_STEPS steps and double up to
 # chunk_steps, so the device starts after a small first chunk (the sweep's
 # all-grid phase draws ~31 000 tracks a step: 268 steps of them were ~50 ms
-# of host sampling ahead of the first launch).
+# of host sampling ahead of the first launch). A chunk also holds at most
+# MAX_CHUNK_TRACKS tracks (one step at least), which bounds the pinned
+# staging buffers the chunks are sampled into.
 FIRST_CHUNK_STEPS = 16
+MAX_CHUNK_TRACKS = 1 << 20
 
 
-def _ramp_chunks(phases, chunk_steps: int, first: int = FIRST_CHUNK_STEPS):
+def _ramp_chunks(phases, chunk_steps: int, first: int = FIRST_CHUNK_STEPS, step_tracks=None,
+                 max_tracks: int = MAX_CHUNK_TRACKS):
     """Chunks (c0, c1, phase table + phase_start) of the ``phases`` of a
     batched run: every global step once, in order, no chunk across a phase
     boundary, sizes from ``min(first, chunk_steps)`` doubling up to
-    ``chunk_steps`` over the run."""
+    ``chunk_steps`` over the run; with ``step_tracks`` (tracks of each global
+    step) a chunk of more than one step holds at most ``max_tracks``."""
     out = []
     size = max(1, min(int(first), int(chunk_steps)))
+    cum = None
+    if step_tracks is not None:
+        cum = np.zeros(len(step_tracks) + 1, dtype=np.int64)
+        np.cumsum(np.asarray(step_tracks, dtype=np.int64), out=cum[1:])
     for s0, s1, tab in phases:
         c0 = s0
         while c0 < s1:
             c1 = min(c0 + size, s1)
+            if cum is not None and cum[c1] - cum[c0] > max_tracks:
+                # the last step end within the budget, one step at least
+                c1 = max(c0 + 1, int(np.searchsorted(cum, cum[c0] + max_tracks, side="right")) - 1)
             out.append((c0, c1, dict(tab, phase_start=s0)))
             c0 = c1
             size = min(2 * size, int(chunk_steps))
@@ -593,7 +605,7 @@ def run_batched_b200(
     stt_dev = torch.from_numpy(np.ascontiguousarray(step_tracks, dtype=np.int64)).to(dev)
     # chunks of global steps (a ramp from FIRST_CHUNK_STEPS); chunk (c0, c1)
     # needs grid c's tracks [offsets[c][min(c0, T_c)], offsets[c][min(c1, T_c)])
-    chunks = _ramp_chunks(phases, int(chunk_steps))
+    chunks = _ramp_chunks(phases, int(chunk_steps), step_tracks=step_tracks)
 
     def jobs_of(c0, c1):
         out = []

@@ -105,6 +105,21 @@ def test_chunks_ramp_up_and_cover_every_step_once():
         for c0, c1, tab in chunks:
             assert c1 - c0 == min(size, starts[tab["phase_start"]] - c0)
             size = min(2 * size, chunk_steps)
+    # with the steps' track counts: at most max_tracks a chunk (one step at
+    # least), as long as the track budget allows, and still every step once
+    rng = np.random.default_rng(5)
+    stt = rng.integers(0, 40_000, size=phases[-1][1])
+    for max_tracks in (1, 50_000, 1 << 20):
+        chunks = b._ramp_chunks(tabs, 512, step_tracks=stt, max_tracks=max_tracks)
+        assert chunks[0][0] == 0 and chunks[-1][1] == phases[-1][1]
+        assert all(x[1] == y[0] for x, y in zip(chunks, chunks[1:]))
+        for c0, c1, tab in chunks:
+            n = int(stt[c0:c1].sum())
+            assert c1 - c0 == 1 or n <= max_tracks
+            assert c1 - c0 <= 512 and c1 <= starts[tab["phase_start"]]
+            if c1 < starts[tab["phase_start"]] and c1 - c0 < 512:
+                # cut by the budget or the ramp, not shorter than either allows
+                assert n + int(stt[c1]) > max_tracks or c1 - c0 >= b.FIRST_CHUNK_STEPS
 
 
 def test_work_tables_cover_each_active_grid_once():
