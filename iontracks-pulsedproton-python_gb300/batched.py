@@ -3,9 +3,10 @@
 ``run_batched_b200(configs)`` returns one reference :class:`Result` per
 configuration -- the same results ``run_simulation_b200`` gives for each of
 them alone -- but advances all grids together (the track centres drawn on the
-host one chunk of global steps ahead of the device, feeder.py): each global step is one
-deposition launch over the step's tracks of every grid and one fused-step
-launch over every active grid (``pic_batched_segment``). The grids may differ
+host one chunk of global steps ahead of the device, feeder.py): each global
+step is one fused-step launch over every active grid, and the tracks of every
+grid are deposited in binned tiles, one launch pair per group of up to eight
+global steps (``pic_batched_segment``). The grids may differ
 in every respect: size, voltage and gap (hence time step and coefficients),
 dose rate, pulse length, step count, wall, seed.
 
@@ -19,11 +20,11 @@ from a fixed meta-seed.
 from __future__ import annotations
 
 import copy
-import os
-from concurrent.futures import ThreadPoolExecutor
 import ctypes
+import os
 import threading
 import warnings
+from concurrent.futures import ThreadPoolExecutor
 from time import perf_counter
 from typing import Optional, Sequence
 
